@@ -1,0 +1,345 @@
+"""FastLoad SpMV benchmark (one JSON line on rank 0).
+
+Workload: the plain FP64 FastLoad SpMV at scale -- square n = 1,048,576,
+column degrees Zipf(1.8) capped at 50,000 (about 20-27M nonzeros, seed 2),
+distinct uniform rows, values N(0,1), x U[-1,1].  A step is one y = A x over
+the whole matrix (y zeroed, then the FastLoad kernel) with the layout and
+sorted x resident in HBM.
+
+metric/unit: achieved SpMV bandwidth in GB/s by the algorithmic byte count
+B = nnz*(8+4) + (n+1)*4 + n*8 + m*8 (FP64 values, int32 rows, FP64 x and y),
+with GFLOP/s (2 nnz per SpMV), % of the measured HBM peak and the relative
+error against the compensated CPU FP64 oracle reported beside it.
+
+--impl reference times the reference's CPU implementation of the path (the
+oracle's port of FastLoad_cpu, src/FastLoad_CPU.h:19-31, spread over all host
+threads with atomic y updates as in test.cu:46-57) on bounded samples of the
+same workload.  Under torchrun (N > 1) every rank runs an independent
+replica (the path has no exchange step); rank 0 prints.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "SpMV HBM GB/s (% of peak) and GFLOP/s vs plain FP64 kernel at stated error"
+SEED = 2
+N_COLS = 1 << 20
+WORKLOAD = "fastload_fp64_zipf1.8_n1048576_cap50000"
+DATA = ("synthetic: seeded Zipf(1.8) column degrees capped at 50,000, distinct uniform rows, N(0,1) values, "
+        "U[-1,1] x (stands in for the SuiteSparse matrices the reference is run on)")
+
+
+def algorithmic_bytes(m, n, nnz, s_val=8, s_idx=4, s_x=8, s_y=8, k=1):
+    return nnz * (s_val + s_idx) + (n + 1) * 4 + k * n * s_x + k * m * s_y
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel, workload):
+    """Per-launch DRAM bytes of `kernel` from the committed ncu summary
+    (profiles/ncu_traffic.txt: '<kernel> <workload> <bytes>' lines)."""
+    p = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
+    if not os.path.exists(p):
+        return None
+    for ln in open(p):
+        f = ln.split()
+        if len(f) >= 3 and f[0] == kernel and f[1] == workload:
+            return float(f[2])
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi SM clock / throttle sampling while the timed region runs."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_bench_{os.getpid()}.csv")
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "50"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            time.sleep(0.1)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self, t0, t1):
+        if self.proc is None or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        for ln in open(self.path):
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                rows.append((float(f[1]), float(f[2]), f[5:9]))
+            except ValueError:
+                continue
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for _, _, r in rows for i, v in enumerate(r) if v.lower() == "active"})
+        busy = [s for s, _, _ in rows]
+        return {"sm_mhz": float(np.median(busy)), "sm_max_mhz": max(x for _, x, _ in rows), "reasons": reasons,
+                "samples": len(rows)}
+
+
+def make_workload():
+    from fastload_gb300 import gen
+
+    return gen.zipf_columns(N_COLS, 1.8, 50000, seed=SEED)
+
+
+def cpu_baseline_sample(c, budget_s=12.0, threads=1):
+    """Times the oracle's FastLoad_cpu port over whole passes of the matrix
+    for about budget_s seconds; returns GB/s by the same byte count."""
+    import oracle
+
+    lay = oracle.build(c.m, c.n, csc=(c.colptr, c.rowidx, c.val), x=c.x)
+    B = algorithmic_bytes(c.m, c.n, c.nnz)
+    passes, t = 0, 0.0
+    used = 1
+    while t < budget_s or passes == 0:
+        t0 = time.perf_counter()
+        if threads == 1:
+            oracle.fastload_spmv(lay, lay["sortx"], c.m)
+        else:
+            _, used = oracle.fastload_spmv(lay, lay["sortx"], c.m, threads=threads)
+        t += time.perf_counter() - t0
+        passes += 1
+        if passes >= 200:
+            break
+    return {"value": B * passes / t / 1e9, "unit": "GB/s", "cores": used, "kind": "port",
+            "sample": f"{passes} full passes of the FastLoad_cpu tile loop (src/FastLoad_CPU.h:19-31) over the "
+                      f"same matrix ({c.nnz} nonzeros), {t:.1f} s"}
+
+
+def run_reference(args, rank, world):
+    """--impl reference: the CPU implementation on all host threads."""
+    if rank != 0:
+        return
+    import oracle
+
+    c = make_workload()
+    lay = oracle.build(c.m, c.n, csc=(c.colptr, c.rowidx, c.val), x=c.x)
+    T = int(lay["tilenum"])
+    # each step: a bounded, rotating sample of about 1/16 of the tiles
+    nsamp = 16
+    cuts = np.searchsorted(lay["tile_ptr"], np.linspace(0, c.nnz, nsamp + 1).astype(np.int64))
+    cuts[0], cuts[-1] = 0, T
+    threads = os.cpu_count() or 1
+
+    def step(i):
+        a, b = int(cuts[i % nsamp]), int(cuts[i % nsamp + 1])
+        sub = {"tilenum": b - a, "tile_ptr": lay["tile_ptr"][a:b + 1] - 0, "tile_len": lay["tile_len"][a:b],
+               "tile_colidx": lay["tile_colidx"][a:b], "sortrowidx": lay["sortrowidx"], "sortval": lay["sortval"]}
+        y, used = oracle.fastload_spmv(sub, lay["sortx"], c.m, threads=threads)
+        return int(lay["tile_ptr"][b] - lay["tile_ptr"][a]), used
+
+    for i in range(args.warmup):
+        step(i)
+    nz_total, used = 0, 1
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        nz, used = step(i)
+        nz_total += nz
+    t = time.perf_counter() - t0
+    frac = nz_total / c.nnz
+    B = algorithmic_bytes(c.m, c.n, c.nnz) * frac
+    gbs = B / t / 1e9
+    line = {"impl": "reference", "metric": METRIC, "value": gbs, "unit": "GB/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": DATA,
+            "config": {"workload": WORKLOAD, "n": c.n, "nnz": c.nnz, "seed": SEED},
+            "cpu_baseline": {"value": gbs, "unit": "GB/s", "cores": used, "kind": "port",
+                             "sample": f"{args.steps} steps, each 1/{nsamp} of the tiles in turn, FastLoad_cpu "
+                                       f"tile loop on {used} OpenMP threads with atomic y updates"},
+            "e2e": {"value": gbs, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args, rank, world):
+    import torch
+
+    import fastload_gb300 as fl
+    import oracle
+
+    dev = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(dev)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    c = make_workload()
+    m, n, nnz = c.m, c.n, c.nnz
+    B = algorithmic_bytes(m, n, nnz)
+    stream = torch.cuda.current_stream()
+    t0 = time.perf_counter()
+    plan = fl.Plan.from_csc(m, n, c.colptr, c.rowidx, c.val, with_reference_arrays=True)
+    torch.cuda.synchronize()
+    prep_s = time.perf_counter() - t0
+    x = torch.from_numpy(c.x).cuda()
+    xs = plan.permute_x(x)
+    y = torch.zeros(m, dtype=torch.float64, device="cuda")
+    kernel = fl.KERNEL_AUTO
+
+    # error statement against the compensated FP64 oracle
+    ydd = oracle.csc_spmv_dd(m, n, c.colptr, c.rowidx, c.val, c.x)
+    plan.spmv(xs, y)
+    rel = oracle.rel_errors(y.cpu().numpy(), ydd)
+
+    def step():
+        y.zero_()
+        plan.spmv(xs, y, accumulate=True, kernel=kernel)
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+    K = args.steps
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(dev) as clk:
+        wall0 = time.time()
+        start.record(stream)
+        for i in range(K):
+            y.zero_()
+            ev[i][0].record(stream)
+            plan.spmv(xs, y, accumulate=True, kernel=kernel)
+            ev[i][1].record(stream)
+        end.record(stream)
+        torch.cuda.synchronize()
+        wall1 = time.time()
+    if dist:
+        dist.barrier()
+    total_ms = start.elapsed_time(end)
+    kern_ms = float(np.mean([a.elapsed_time(b) for a, b in ev]))
+    if dist:
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_step = total_ms / K
+    peak, peak_kind = measured_peaks()
+    value = B * world / (ms_step * 1e-3) / 1e9
+    achieved = B / (kern_ms * 1e-3) / 1e9
+
+    # the reference-design kernel (one warp per tile) on the same inputs
+    def time_kernel(kern, reps=50):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        for _ in range(3):
+            plan.spmv(xs, y, kernel=kern)
+        ts = []
+        for _ in range(reps):
+            y.zero_()
+            a.record(stream)
+            plan.spmv(xs, y, accumulate=True, kernel=kern)
+            b.record(stream)
+            b.synchronize()
+            ts.append(a.elapsed_time(b))
+        return float(np.mean(ts))
+
+    variants = {name: B / (time_kernel(k) * 1e-3) / 1e9 for name, k in
+                (("tile", fl.KERNEL_TILE), ("stream1", fl.KERNEL_STREAM), ("stream2", fl.KERNEL_STREAM2))}
+
+    # end to end through the host-buffer C-ABI call: H2D of x, SpMV, D2H of y
+    hx = torch.from_numpy(np.ascontiguousarray(plan.permute_x(x).cpu().numpy())).pin_memory().numpy()
+    hy = torch.empty(m, dtype=torch.float64).pin_memory().numpy()
+    for _ in range(3):
+        plan.spmv_host(hx, hy, kernel=kernel)
+    ke = max(10, min(K, 200))
+    t0 = time.perf_counter()
+    for _ in range(ke):
+        plan.spmv_host(hx, hy, kernel=kernel)
+    e2e_s = (time.perf_counter() - t0) / ke
+    e2e_rel = oracle.rel_errors(hy, ydd)
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+    cpu = cpu_baseline_sample(c) if world == 1 else None
+    traffic = ncu_traffic("k_spmv_stream_f64", WORKLOAD)
+    line = {
+        "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": K, "warmup": args.warmup,
+        "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": DATA,
+        "config": {"workload": WORKLOAD, "m": m, "n": n, "nnz": nnz, "seed": SEED, "kernel": "stream (auto)",
+                   "tilenum": plan.info["tilenum"], "steps_h_count": plan.info["steps"],
+                   "l2": "inputs larger than L2: matrix streams %.0f MB vs 129 MB L2" % (nnz * 12 / 1e6),
+                   "parallelism": f"replicas x{world}"},
+        "pct_of_peak": 100.0 * value / world / peak,
+        "gflops": 2.0 * nnz * world / (ms_step * 1e-3) / 1e9,
+        "rel_err_vs_fp64_oracle": {"normwise": rel[0], "max_over_inf": rel[1]},
+        "kernel_variants_gbs": variants,
+        "preprocess_s": prep_s,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic, "peak_kind": f"{peak_kind} hbm_gbs",
+                     "kernel": "k_spmv_stream_f64", "bytes_per_launch": B, "kernel_ms": kern_ms},
+        "cpu_baseline": cpu,
+        "e2e": {"value": B / e2e_s / 1e9, "unit": "GB/s", "h2d_bytes_per_step": n * 8, "d2h_bytes_per_step": m * 8,
+                "ms_per_step": e2e_s * 1e3, "call": "fl_plan_spmv_host (pinned host x and y)",
+                "rel_err": e2e_rel[0]},
+        "gpu_launches": K,
+        "clocks": clk.summary(wall0, wall1),
+    }
+    print(json.dumps(line), flush=True)
+    plan.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="fastload", choices=["fastload", "reference"])
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", args.gpus if args.gpus == 1 else 1))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_gpu(args, rank, world)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,106 @@
+"""ctypes binding of the C ABI in include/fastload.h.
+
+Loading fails loudly (ImportError) when the CUDA library has not been built:
+there is no CPU fallback for any entry point.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from . import _build
+
+c_int_p = C.POINTER(C.c_int)
+c_double_p = C.POINTER(C.c_double)
+c_float_p = C.POINTER(C.c_float)
+
+
+class SlideMatrixC(C.Structure):
+    """Same members and order as the reference's slide_matrix
+    (src/format.h:6-20) and fl_slide_matrix."""
+
+    _fields_ = [
+        ("sortval", c_double_p),
+        ("sortrowidx", c_int_p),
+        ("tile_ptr", c_int_p),
+        ("tile_len", c_int_p),
+        ("tile_colidx", c_int_p),
+        ("tile_tall", c_int_p),
+        ("tile_format", c_int_p),
+        ("countrow", c_int_p),
+        ("segmentoffset", c_int_p),
+        ("sortrowindex", c_int_p),
+        ("tilenum", C.c_int),
+        ("segsum", C.c_int),
+    ]
+
+
+class PlanInfoC(C.Structure):
+    _fields_ = [
+        ("m", C.c_int), ("n", C.c_int), ("nnz", C.c_int), ("tilenum", C.c_int), ("steps", C.c_int),
+        ("segsum", C.c_int), ("regions", C.c_int), ("items", C.c_int), ("device_bytes", C.c_size_t),
+    ]
+
+
+# (name, restype, argtypes) of every exported symbol; tests check the .so
+# exports each one and that include/fastload.h declares each one.
+SIGNATURES = [
+    ("fl_last_error", C.c_char_p, []),
+    ("fl_version", C.c_char_p, []),
+    ("fl_device_count", C.c_int, []),
+    ("fl_debug_fail_alloc_after", None, [C.c_int]),
+    ("fl_csr_to_csc", C.c_int, [c_double_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("fl_col_sort", C.c_int, [c_double_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                              C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("fl_format_transform", C.c_int, [c_double_p, c_double_p, C.POINTER(SlideMatrixC), C.c_void_p, C.c_void_p,
+                                      C.c_void_p, C.c_int, C.c_int, C.c_int, c_int_p]),
+    ("fl_fastload_spmv", C.c_int, [C.POINTER(SlideMatrixC), C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                                   C.c_void_p, C.c_int, c_double_p, c_int_p]),
+    ("fl_tile_destroy", None, [C.POINTER(SlideMatrixC)]),
+    ("fl_plan_create_csr", C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                                     C.c_void_p, C.c_int, C.c_void_p]),
+    ("fl_plan_create_csc", C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                                     C.c_void_p, C.c_int, C.c_void_p]),
+    ("fl_plan_info_get", C.c_int, [C.c_void_p, C.POINTER(PlanInfoC)]),
+    ("fl_plan_export", C.c_int, [C.c_void_p, C.POINTER(SlideMatrixC), C.c_void_p]),
+    ("fl_plan_permute_x", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("fl_plan_spmv", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p]),
+    ("fl_plan_spmv_host", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
+    ("fl_plan_destroy", C.c_int, [C.c_void_p]),
+]
+
+_LIB = None
+
+
+def load(path: str | None = None) -> C.CDLL:
+    """Returns the loaded library, raising ImportError when it is missing."""
+    global _LIB
+    if _LIB is not None and path is None:
+        return _LIB
+    p = path or _build.lib_path()
+    if not os.path.exists(p):
+        raise ImportError(f"FastLoad GB300 CUDA library not built ({p} missing); "
+                          "run `python -c 'import __graft_entry__ as g; g.build()'`")
+    lib = C.CDLL(p)
+    for name, res, args in SIGNATURES:
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _LIB = lib
+    return lib
+
+
+class FastLoadError(RuntimeError):
+    """A library call returned a negative status; .code holds it."""
+
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+
+
+def check(rc: int) -> None:
+    if rc != 0:
+        msg = load().fl_last_error()
+        raise FastLoadError(rc, msg.decode() if msg else "")

@@ -1,0 +1,495 @@
+// fl_api.cu -- extern "C" entry points of the FastLoad GB300 library.
+//
+// Reference-compatible host-buffer calls (csr_to_csc, ColSort,
+// formatTransform, FastLoad_spmv) and the device-resident plan API.
+// Every call validates its arguments, returns an int status and never
+// falls back to a CPU path.
+#include "fl_internal.cuh"
+
+#include <cstdlib>
+#include <cstring>
+#include <new>
+
+namespace fl {
+const char *last_error_cstr();
+void debug_fail_alloc_after(int n);
+}  // namespace fl
+
+using namespace fl;
+
+struct fl_plan {
+    Layout L;
+    bool has_ref = false;
+    DevBuf<double> stage_x, stage_y;  // device staging of fl_plan_spmv_host
+};
+
+namespace {
+
+constexpr long kMaxNnz = 0x7fffffffL - 65536;  // headroom for padding and item rounding
+
+int check_sizes(const char *who, int m, int n, int nnz) {
+    if (m < 0 || n < 0 || nnz < 0)
+        return fail(FL_ERR_ARG, "%s: negative size (m=%d n=%d nnz=%d)", who, m, n, nnz);
+    if ((long)nnz > kMaxNnz) return fail(FL_ERR_OVERFLOW, "%s: nnz=%d exceeds the 32-bit index space", who, nnz);
+    return FL_SUCCESS;
+}
+
+template <typename T>
+int upload(DevBuf<T> &d, const T *h, size_t count, cudaStream_t s) {
+    FL_TRY(d.alloc(count, s));
+    if (count) FL_CUDA(cudaMemcpyAsync(d.get(), h, count * sizeof(T), cudaMemcpyHostToDevice, s));
+    return FL_SUCCESS;
+}
+template <typename T>
+int download(T *h, const T *d, size_t count, cudaStream_t s) {
+    if (count) FL_CUDA(cudaMemcpyAsync(h, d, count * sizeof(T), cudaMemcpyDeviceToHost, s));
+    return FL_SUCCESS;
+}
+
+struct Timer {
+    cudaEvent_t a = nullptr, b = nullptr;
+    int start(cudaStream_t s) {
+        FL_CUDA(cudaEventCreate(&a));
+        FL_CUDA(cudaEventCreate(&b));
+        FL_CUDA(cudaEventRecord(a, s));
+        return FL_SUCCESS;
+    }
+    int stop(cudaStream_t s, double *ms) {
+        FL_CUDA(cudaEventRecord(b, s));
+        FL_CUDA(cudaEventSynchronize(b));
+        float f = 0;
+        FL_CUDA(cudaEventElapsedTime(&f, a, b));
+        if (ms) *ms = f;
+        return FL_SUCCESS;
+    }
+    ~Timer() {
+        if (a) cudaEventDestroy(a);
+        if (b) cudaEventDestroy(b);
+    }
+};
+
+template <typename T>
+T *host_alloc(size_t count) {
+    return (T *)calloc(count ? count : 1, sizeof(T));
+}
+
+// D2H of the reference layout into malloc'd arrays of *out.
+int export_layout(const Layout &L, fl_slide_matrix *out, cudaStream_t s) {
+    fl_slide_matrix m;
+    memset(&m, 0, sizeof m);
+    const int T = L.tilenum, S = L.segsum, Z = L.nnz;
+    m.sortval = host_alloc<double>(Z);
+    m.sortrowidx = host_alloc<int>(Z);
+    m.tile_ptr = host_alloc<int>((size_t)T + 1);
+    m.tile_len = host_alloc<int>(T);
+    m.tile_colidx = host_alloc<int>(T);
+    m.tile_tall = host_alloc<int>(T);
+    m.tile_format = host_alloc<int>(T);
+    m.countrow = host_alloc<int>((size_t)T + 1);
+    m.segmentoffset = host_alloc<int>((size_t)S + 1);
+    m.sortrowindex = host_alloc<int>(Z);
+    m.tilenum = T;
+    m.segsum = S;
+    if (!m.sortval || !m.sortrowidx || !m.tile_ptr || !m.tile_len || !m.tile_colidx || !m.tile_tall ||
+        !m.tile_format || !m.countrow || !m.segmentoffset || !m.sortrowindex) {
+        fl_tile_destroy(&m);
+        return fail(FL_ERR_ALLOC, "formatTransform: host allocation failed");
+    }
+    int rc = FL_SUCCESS;
+    if (Z) {
+        if ((rc = download(m.sortval, L.val.get(), Z, s))) goto bad;
+        if ((rc = download(m.sortrowidx, L.row.get(), Z, s))) goto bad;
+        if ((rc = download(m.sortrowindex, L.sortrowindex.get(), Z, s))) goto bad;
+    }
+    if ((rc = download(m.tile_ptr, L.tile_ptr.get(), (size_t)T + 1, s))) goto bad;
+    if ((rc = download(m.countrow, L.countrow.get(), (size_t)T + 1, s))) goto bad;
+    if ((rc = download(m.segmentoffset, L.segmentoffset.get(), (size_t)S + 1, s))) goto bad;
+    if (T) {
+        if ((rc = download(m.tile_len, L.tile_len.get(), T, s))) goto bad;
+        if ((rc = download(m.tile_colidx, L.tile_colidx.get(), T, s))) goto bad;
+        if ((rc = download(m.tile_format, L.tile_format.get(), T, s))) goto bad;
+    }
+    {
+        cudaError_t e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) {
+            rc = fail(FL_ERR_CUDA, "formatTransform: copy-back failed: %s", cudaGetErrorString(e));
+            goto bad;
+        }
+    }
+    *out = m;
+    return FL_SUCCESS;
+bad:
+    fl_tile_destroy(&m);
+    return rc;
+}
+
+// Uploads a host slide_matrix into a device layout (for FastLoad_spmv).
+// The step table the streaming kernel needs is re-derived from the tile
+// arrays: sorted column c has as many nonzeros as tiles that cover it, and
+// those counts determine the staircase.  check_tile_meta then confirms the
+// uploaded tile arrays are exactly the staircase's, so deriving columns
+// arithmetically is valid for this matrix.
+__global__ void k_cover_count(int tilenum, const int *tile_colidx, const int *tile_len, int *cnt) {
+    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < tilenum; t += (long)gridDim.x * blockDim.x) {
+        int c = tile_colidx[t], len = tile_len[t];
+        for (int i = 0; i < len; i++) atomicAdd(cnt + c + i, 1);
+    }
+}
+
+__global__ void k_check_layout(int tilenum, int n, int m, int nnz, const int *tile_ptr, const int *tile_len,
+                               const int *tile_colidx, const int *row, int *err) {
+    long tid = blockIdx.x * (long)blockDim.x + threadIdx.x, stride = (long)gridDim.x * blockDim.x;
+    int e = 0;
+    for (long t = tid; t < tilenum; t += stride) {
+        int len = tile_len[t], c = tile_colidx[t];
+        if (len < 1 || len > 32 || c < 0 || c + len > n) e |= 1;
+        if (tile_ptr[t + 1] - tile_ptr[t] != len) e |= 2;
+    }
+    for (long p = tid; p < nnz; p += stride) {
+        int r = row[p];
+        if (r < 0 || r >= m) e |= 4;
+    }
+    if (tid == 0 && (tile_ptr[0] != 0 || tile_ptr[tilenum] != nnz)) e |= 8;
+    if (e) atomicOr(err, e);
+}
+
+int upload_layout(Layout &L, const fl_slide_matrix *mat, int m, int n, int nnz, cudaStream_t s) {
+    const int T = mat->tilenum;
+    if (T < 0) return fail(FL_ERR_ARG, "FastLoad_spmv: tilenum=%d", T);
+    if (nnz > 0 && (!mat->sortval || !mat->sortrowidx || !mat->tile_ptr || !mat->tile_len || !mat->tile_colidx))
+        return fail(FL_ERR_ARG, "FastLoad_spmv: slide_matrix has NULL arrays");
+    L.m = m;
+    L.n = n;
+    L.nnz = nnz;
+    L.tilenum = T;
+    size_t np = padded(nnz);
+    FL_TRY(L.row.alloc(np, s));
+    FL_TRY(L.val.alloc(np, s));
+    FL_CUDA(cudaMemsetAsync(L.row.get() + nnz, 0xff, (np - nnz) * sizeof(int), s));
+    FL_CUDA(cudaMemsetAsync(L.val.get() + nnz, 0, (np - nnz) * sizeof(double), s));
+    if (nnz) {
+        FL_CUDA(cudaMemcpyAsync(L.row.get(), mat->sortrowidx, (size_t)nnz * sizeof(int), cudaMemcpyHostToDevice, s));
+        FL_CUDA(cudaMemcpyAsync(L.val.get(), mat->sortval, (size_t)nnz * sizeof(double), cudaMemcpyHostToDevice, s));
+    }
+    DevBuf<int> tptr, tlen, tcol, cnt, err;
+    FL_TRY(upload(tptr, mat->tile_ptr, (size_t)T + 1, s));
+    FL_TRY(upload(tlen, mat->tile_len, T, s));
+    FL_TRY(upload(tcol, mat->tile_colidx, T, s));
+    FL_TRY(err.alloc(1, s));
+    FL_CUDA(cudaMemsetAsync(err.get(), 0, sizeof(int), s));
+    k_check_layout<<<256, 256, 0, s>>>(T, n, m, nnz, tptr.get(), tlen.get(), tcol.get(), L.row.get(), err.get());
+    FL_CUDA(cudaGetLastError());
+    int herr = 0;
+    FL_TRY(download(&herr, err.get(), 1, s));
+    FL_CUDA(cudaStreamSynchronize(s));
+    if (herr) return fail(FL_ERR_ARG, "FastLoad_spmv: slide_matrix is not a valid FastLoad layout for "
+                                      "colA=%d rowA=%d nnz=%d (flags 0x%x)", n, m, nnz, herr);
+    // nnz per sorted column from tile coverage, then the step table
+    FL_TRY(cnt.alloc((size_t)n + 1, s));
+    if (n) FL_CUDA(cudaMemsetAsync(cnt.get(), 0, (size_t)n * sizeof(int), s));
+    if (T) {
+        k_cover_count<<<256, 256, 0, s>>>(T, tcol.get(), tlen.get(), cnt.get());
+        FL_CUDA(cudaGetLastError());
+    }
+    FL_TRY(build_steps(L, m, n, nnz, cnt.get(), s));
+    if (L.tilenum != T) return fail(FL_ERR_ARG, "FastLoad_spmv: tilenum=%d but the tiles imply %d", T, L.tilenum);
+    FL_TRY(check_tile_meta(L, tptr.get(), tlen.get(), tcol.get(), s));
+    return FL_SUCCESS;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *fl_last_error(void) { return last_error_cstr(); }
+const char *fl_version(void) { return "fastload_gb300 0.1 (sm_103a)"; }
+int fl_device_count(void) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+void fl_debug_fail_alloc_after(int countdown) { debug_fail_alloc_after(countdown); }
+
+int fl_csr_to_csc(double *time_ms, int m, int n, int nnz, const double *csr_val, const int *csr_row_ptr,
+                  const int *csr_col_ind, double *csc_val, int *csc_row_ind, int *csc_col_ptr, int *nnzpercol) {
+    clear_error();
+    FL_TRY(check_sizes("csr_to_csc", m, n, nnz));
+    if (!csr_row_ptr || !csc_col_ptr || !nnzpercol || (nnz && (!csr_val || !csr_col_ind || !csc_val || !csc_row_ind)))
+        return fail(FL_ERR_ARG, "csr_to_csc: NULL array");
+    cudaStream_t s = 0;
+    DevBuf<int> rp, ci, cp, cr, npc;
+    DevBuf<double> v, cv;
+    FL_TRY(upload(rp, csr_row_ptr, (size_t)m + 1, s));
+    FL_TRY(upload(ci, csr_col_ind, nnz, s));
+    FL_TRY(upload(v, csr_val, nnz, s));
+    FL_TRY(cp.alloc((size_t)n + 1, s));
+    FL_TRY(cr.alloc(nnz, s));
+    FL_TRY(cv.alloc(nnz, s));
+    FL_TRY(npc.alloc(n, s));
+    Timer t;
+    FL_TRY(t.start(s));
+    FL_TRY(csr_to_csc_device(m, n, nnz, rp.get(), ci.get(), v.get(), cp.get(), cr.get(), cv.get(), npc.get(), s));
+    FL_TRY(t.stop(s, time_ms));
+    FL_TRY(download(csc_col_ptr, cp.get(), (size_t)n + 1, s));
+    FL_TRY(download(nnzpercol, npc.get(), n, s));
+    FL_TRY(download(csc_row_ind, cr.get(), nnz, s));
+    FL_TRY(download(csc_val, cv.get(), nnz, s));
+    FL_CUDA(cudaStreamSynchronize(s));
+    return FL_SUCCESS;
+}
+
+int fl_col_sort(double *time_ms, int rowA, int colA, int nnz, const int *nnzPerCol, const int *cscColPtr,
+                const int *cscRowIdx, const double *cscVal, int *sortrowidxTmp, double *sortvalTmp, int *sortnnzTmp,
+                const double *x, double *sortx) {
+    clear_error();
+    FL_TRY(check_sizes("ColSort", rowA, colA, nnz));
+    if ((colA && (!nnzPerCol || !cscColPtr || !sortnnzTmp)) ||
+        (nnz && (!cscRowIdx || !cscVal || !sortrowidxTmp || !sortvalTmp)) || (colA && x && !sortx))
+        return fail(FL_ERR_ARG, "ColSort: NULL array");
+    cudaStream_t s = 0;
+    DevBuf<int> cnt, cp, cr, perm, snnz, srow;
+    DevBuf<double> cv, dx, dxs, sval;
+    FL_TRY(upload(cnt, nnzPerCol, colA, s));
+    FL_TRY(upload(cp, cscColPtr, (size_t)colA + 1, s));
+    FL_TRY(upload(cr, cscRowIdx, nnz, s));
+    FL_TRY(upload(cv, cscVal, nnz, s));
+    if (x) {
+        FL_TRY(upload(dx, x, colA, s));
+        FL_TRY(dxs.alloc(colA, s));
+    }
+    FL_TRY(perm.alloc(colA, s));
+    FL_TRY(snnz.alloc(colA, s));
+    FL_TRY(srow.alloc(nnz, s));
+    FL_TRY(sval.alloc(nnz, s));
+    Timer t;
+    FL_TRY(t.start(s));
+    FL_TRY(col_sort_device(colA, nnz, cnt.get(), cp.get(), cr.get(), cv.get(), x ? dx.get() : nullptr, perm.get(),
+                           snnz.get(), srow.get(), sval.get(), x ? dxs.get() : nullptr, s));
+    FL_TRY(t.stop(s, time_ms));
+    FL_TRY(download(sortnnzTmp, snnz.get(), colA, s));
+    FL_TRY(download(sortrowidxTmp, srow.get(), nnz, s));
+    FL_TRY(download(sortvalTmp, sval.get(), nnz, s));
+    if (x) FL_TRY(download(sortx, dxs.get(), colA, s));
+    FL_CUDA(cudaStreamSynchronize(s));
+    return FL_SUCCESS;
+}
+
+int fl_format_transform(double *time_tran_ms, double *time_class_ms, fl_slide_matrix *matrix,
+                        const int *sortrowidx_tmp, const double *sortval_tmp, const int *sortnnz_tmp, int nnz,
+                        int rowA, int colA, int *h_count) {
+    clear_error();
+    FL_TRY(check_sizes("formatTransform", rowA, colA, nnz));
+    if (!matrix || (colA && !sortnnz_tmp) || (nnz && (!sortrowidx_tmp || !sortval_tmp)))
+        return fail(FL_ERR_ARG, "formatTransform: NULL argument");
+    cudaStream_t s = 0;
+    DevBuf<int> snnz, srow;
+    DevBuf<double> sval;
+    FL_TRY(upload(snnz, sortnnz_tmp, colA, s));
+    FL_TRY(upload(srow, sortrowidx_tmp, nnz, s));
+    FL_TRY(upload(sval, sortval_tmp, nnz, s));
+    Layout L;
+    float a = 0, b = 0;
+    FL_TRY(build_layout_device(L, rowA, colA, nnz, snnz.get(), srow.get(), sval.get(), true, s, &a, &b));
+    if (time_tran_ms) *time_tran_ms = a;
+    if (time_class_ms) *time_class_ms = b;
+    if (h_count) *h_count = L.st.steps;
+    return export_layout(L, matrix, s);
+}
+
+int fl_fastload_spmv(const fl_slide_matrix *matrix, int nnz, int colA, int rowA, const double *x_sorted, double *y,
+                     const double *y_golden, int reps, double *ms_per_spmv, int *mismatches) {
+    clear_error();
+    FL_TRY(check_sizes("FastLoad_spmv", rowA, colA, nnz));
+    if (!matrix || (colA && !x_sorted) || (rowA && !y)) return fail(FL_ERR_ARG, "FastLoad_spmv: NULL argument");
+    if (reps < 0) return fail(FL_ERR_ARG, "FastLoad_spmv: reps=%d", reps);
+    cudaStream_t s = 0;
+    Layout L;
+    FL_TRY(upload_layout(L, matrix, rowA, colA, nnz, s));
+    DevBuf<double> dx, dy;
+    FL_TRY(upload(dx, x_sorted, colA, s));
+    FL_TRY(dy.alloc(rowA, s));
+    if (rowA) FL_CUDA(cudaMemsetAsync(dy.get(), 0, (size_t)rowA * sizeof(double), s));
+    FL_TRY(spmv_stream_f64(L, dx.get(), dy.get(), FL_KERNEL_AUTO, s));  // untimed first run
+    double total = 0;
+    for (int r = 0; r < reps; r++) {
+        if (rowA) FL_CUDA(cudaMemsetAsync(dy.get(), 0, (size_t)rowA * sizeof(double), s));
+        Timer t;
+        double ms = 0;
+        FL_TRY(t.start(s));
+        FL_TRY(spmv_stream_f64(L, dx.get(), dy.get(), FL_KERNEL_AUTO, s));
+        FL_TRY(t.stop(s, &ms));
+        total += ms;
+    }
+    if (reps == 0 && rowA) {
+        FL_CUDA(cudaMemsetAsync(dy.get(), 0, (size_t)rowA * sizeof(double), s));
+        FL_TRY(spmv_stream_f64(L, dx.get(), dy.get(), FL_KERNEL_AUTO, s));
+    }
+    FL_TRY(download(y, dy.get(), rowA, s));
+    FL_CUDA(cudaStreamSynchronize(s));
+    if (ms_per_spmv) *ms_per_spmv = reps ? total / reps : 0.0;
+    if (mismatches) {
+        int bad = 0;
+        if (y_golden)
+            for (int i = 0; i < rowA; i++) {
+                double d = y_golden[i] - y[i];
+                if (d < 0) d = -d;
+                double a = y[i] < 0 ? -y[i] : y[i];
+                if (d > 0.01 * a) bad++;
+            }
+        *mismatches = bad;
+    }
+    return FL_SUCCESS;
+}
+
+void fl_tile_destroy(fl_slide_matrix *m) {
+    if (!m) return;
+    free(m->sortval);
+    free(m->sortrowidx);
+    free(m->tile_ptr);
+    free(m->tile_len);
+    free(m->tile_colidx);
+    free(m->tile_tall);
+    free(m->tile_format);
+    free(m->countrow);
+    free(m->segmentoffset);
+    free(m->sortrowindex);
+    memset(m, 0, sizeof *m);
+}
+
+// ------------------------------------------------------------ plan API --
+static int plan_from_csc(fl_plan_t *out, int m, int n, int nnz, const int *colptr, const int *rowidx,
+                         const double *val, int with_ref, cudaStream_t s) {
+    fl_plan *p = new (std::nothrow) fl_plan();
+    if (!p) return fail(FL_ERR_ALLOC, "plan: host allocation failed");
+    DevBuf<int> cnt, snnz, srow;
+    DevBuf<double> sval;
+    int rc = FL_SUCCESS;
+    auto bail = [&](int code) {
+        delete p;
+        return code;
+    };
+    if ((rc = cnt.alloc(n, s))) return bail(rc);
+    if ((rc = p->L.perm.alloc(n, s))) return bail(rc);
+    if ((rc = p->L.sortnnz.alloc(n, s))) return bail(rc);
+    if ((rc = srow.alloc(nnz, s))) return bail(rc);
+    if ((rc = sval.alloc(nnz, s))) return bail(rc);
+    if ((rc = counts_from_ptr(colptr, n, cnt.get(), s))) return bail(rc);
+    if ((rc = col_sort_device(n, nnz, cnt.get(), colptr, rowidx, val, nullptr, p->L.perm.get(), p->L.sortnnz.get(),
+                              srow.get(), sval.get(), nullptr, s)))
+        return bail(rc);
+    if ((rc = build_layout_device(p->L, m, n, nnz, p->L.sortnnz.get(), srow.get(), sval.get(), with_ref != 0, s,
+                                  nullptr, nullptr)))
+        return bail(rc);
+    p->has_ref = with_ref != 0;
+    cudaError_t e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return bail(fail(FL_ERR_CUDA, "plan: %s", cudaGetErrorString(e)));
+    *out = p;
+    return FL_SUCCESS;
+}
+
+int fl_plan_create_csc(fl_plan_t *plan, int m, int n, int nnz, const int *d_colptr, const int *d_rowidx,
+                       const double *d_val, int with_reference_arrays, void *stream) {
+    clear_error();
+    if (!plan) return fail(FL_ERR_ARG, "plan_create_csc: NULL plan pointer");
+    *plan = nullptr;
+    FL_TRY(check_sizes("plan_create_csc", m, n, nnz));
+    if (!d_colptr || (nnz && (!d_rowidx || !d_val))) return fail(FL_ERR_ARG, "plan_create_csc: NULL array");
+    FL_TRY(check_index_range(d_rowidx, nnz, m, "plan_create_csc: row index", (cudaStream_t)stream));
+    return plan_from_csc(plan, m, n, nnz, d_colptr, d_rowidx, d_val, with_reference_arrays, (cudaStream_t)stream);
+}
+
+int fl_plan_create_csr(fl_plan_t *plan, int m, int n, int nnz, const int *d_rowptr, const int *d_colidx,
+                       const double *d_val, int with_reference_arrays, void *stream) {
+    clear_error();
+    if (!plan) return fail(FL_ERR_ARG, "plan_create_csr: NULL plan pointer");
+    *plan = nullptr;
+    FL_TRY(check_sizes("plan_create_csr", m, n, nnz));
+    if (!d_rowptr || (nnz && (!d_colidx || !d_val))) return fail(FL_ERR_ARG, "plan_create_csr: NULL array");
+    cudaStream_t s = (cudaStream_t)stream;
+    DevBuf<int> cp, cr, npc;
+    DevBuf<double> cv;
+    FL_TRY(cp.alloc((size_t)n + 1, s));
+    FL_TRY(cr.alloc(nnz, s));
+    FL_TRY(cv.alloc(nnz, s));
+    FL_TRY(npc.alloc(n, s));
+    FL_TRY(csr_to_csc_device(m, n, nnz, d_rowptr, d_colidx, d_val, cp.get(), cr.get(), cv.get(), npc.get(), s));
+    return plan_from_csc(plan, m, n, nnz, cp.get(), cr.get(), cv.get(), with_reference_arrays, s);
+}
+
+int fl_plan_info_get(fl_plan_t p, fl_plan_info *info) {
+    clear_error();
+    if (!p || !info) return fail(FL_ERR_ARG, "plan_info: NULL argument");
+    const Layout &L = p->L;
+    info->m = L.m;
+    info->n = L.n;
+    info->nnz = L.nnz;
+    info->tilenum = L.tilenum;
+    info->steps = L.st.steps;
+    info->segsum = p->has_ref ? L.segsum : -1;
+    info->regions = L.regions.nregions;
+    info->items = L.regions.nitems;
+    size_t b = L.row.n * 4 + L.val.n * 8 + L.perm.n * 4 + L.sortnnz.n * 4 + L.tile_ptr.n * 4 + L.tile_len.n * 4 +
+               L.tile_colidx.n * 4 + L.tile_format.n * 4 + L.sortrowindex.n * 4 + L.countrow.n * 4 +
+               L.segmentoffset.n * 4 + L.regions.region.n * sizeof(RegionDesc) +
+               L.regions.item.n * sizeof(ItemDesc) + 5 * (size_t)(L.st.steps + 1) * 4;
+    info->device_bytes = b;
+    return FL_SUCCESS;
+}
+
+int fl_plan_export(fl_plan_t p, fl_slide_matrix *matrix, int *perm) {
+    clear_error();
+    if (!p || !matrix) return fail(FL_ERR_ARG, "plan_export: NULL argument");
+    if (!p->has_ref) return fail(FL_ERR_ARG, "plan_export: plan was built without reference arrays");
+    cudaStream_t s = 0;
+    FL_CUDA(cudaDeviceSynchronize());
+    if (perm && p->L.n) {
+        FL_TRY(download(perm, p->L.perm.get(), p->L.n, s));
+        FL_CUDA(cudaStreamSynchronize(s));
+    }
+    return export_layout(p->L, matrix, s);
+}
+
+int fl_plan_permute_x(fl_plan_t p, const double *d_x, double *d_xs, void *stream) {
+    clear_error();
+    if (!p || (p->L.n && (!d_x || !d_xs))) return fail(FL_ERR_ARG, "plan_permute_x: NULL argument");
+    return permute_x(p->L.perm.get(), p->L.n, d_x, d_xs, (cudaStream_t)stream);
+}
+
+int fl_plan_spmv(fl_plan_t p, const double *d_xs, double *d_y, int accumulate, int variant, void *stream) {
+    if (!p || (p->L.n && !d_xs) || (p->L.m && !d_y)) return fail(FL_ERR_ARG, "plan_spmv: NULL argument");
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!accumulate && p->L.m) FL_CUDA(cudaMemsetAsync(d_y, 0, (size_t)p->L.m * sizeof(double), s));
+    switch (variant) {
+        case FL_KERNEL_AUTO:
+        case FL_KERNEL_STREAM:
+        case FL_KERNEL_STREAM2: return spmv_stream_f64(p->L, d_xs, d_y, variant, s);
+        case FL_KERNEL_TILE: return spmv_tile_f64(p->L, d_xs, d_y, s);
+        default: return fail(FL_ERR_ARG, "plan_spmv: unknown kernel variant %d", variant);
+    }
+}
+
+int fl_plan_spmv_host(fl_plan_t p, const double *h_xs, double *h_y, int variant, void *stream) {
+    clear_error();
+    if (!p || (p->L.n && !h_xs) || (p->L.m && !h_y)) return fail(FL_ERR_ARG, "plan_spmv_host: NULL argument");
+    cudaStream_t s = (cudaStream_t)stream;
+    if (p->stage_x.n < (size_t)p->L.n) FL_TRY(p->stage_x.alloc(p->L.n, s));
+    if (p->stage_y.n < (size_t)p->L.m) FL_TRY(p->stage_y.alloc(p->L.m, s));
+    if (p->L.n)
+        FL_CUDA(cudaMemcpyAsync(p->stage_x.get(), h_xs, (size_t)p->L.n * sizeof(double), cudaMemcpyHostToDevice, s));
+    FL_TRY(fl_plan_spmv(p, p->stage_x.get(), p->stage_y.get(), 0, variant, stream));
+    FL_TRY(download(h_y, p->stage_y.get(), p->L.m, s));
+    FL_CUDA(cudaStreamSynchronize(s));
+    return FL_SUCCESS;
+}
+
+int fl_plan_destroy(fl_plan_t p) {
+    if (!p) return FL_SUCCESS;
+    cudaDeviceSynchronize();  // no launch of this plan may still be reading it
+    delete p;
+    return FL_SUCCESS;
+}
+
+}  // extern "C"

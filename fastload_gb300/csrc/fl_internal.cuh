@@ -1,0 +1,178 @@
+// fl_internal.cuh -- shared internals of the FastLoad GB300 library:
+// status handling, device buffers, the device-resident matrix layout and
+// the launchers each translation unit exports to the others.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+#include <stdint.h>
+#include <string>
+
+#include "../../include/fastload.h"
+
+namespace fl {
+
+// ---------------------------------------------------------------- status --
+// Every entry point returns an int status (FL_SUCCESS or a negative code)
+// and leaves a message readable through fl_last_error() on the same thread.
+void set_error(int code, const std::string &msg);
+int fail(int code, const char *fmt, ...);
+void clear_error();
+
+#define FL_CUDA(call)                                                          \
+    do {                                                                       \
+        cudaError_t e_ = (call);                                               \
+        if (e_ != cudaSuccess)                                                 \
+            return ::fl::fail(FL_ERR_CUDA, "%s failed: %s (%s:%d)", #call,     \
+                              cudaGetErrorString(e_), __FILE__, __LINE__);     \
+    } while (0)
+
+#define FL_TRY(expr)                                                           \
+    do {                                                                       \
+        int s_ = (expr);                                                       \
+        if (s_ != FL_SUCCESS) return s_;                                       \
+    } while (0)
+
+// Allocation hook: tests install a countdown that makes the N-th device
+// allocation fail, to exercise the error paths without touching the GPU.
+int dev_alloc(void **p, size_t bytes, cudaStream_t s);
+void dev_free(void *p, cudaStream_t s);
+
+// Owning stream-ordered device buffer.
+template <typename T>
+struct DevBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    cudaStream_t s = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    DevBuf(DevBuf &&o) noexcept : p(o.p), n(o.n), s(o.s) { o.p = nullptr; o.n = 0; }
+    DevBuf &operator=(DevBuf &&o) noexcept {
+        if (this != &o) { release(); p = o.p; n = o.n; s = o.s; o.p = nullptr; o.n = 0; }
+        return *this;
+    }
+    ~DevBuf() { release(); }
+    int alloc(size_t count, cudaStream_t stream) {
+        release();
+        s = stream;
+        n = count;
+        if (count == 0) return FL_SUCCESS;
+        return dev_alloc((void **)&p, count * sizeof(T), stream);
+    }
+    void release() {
+        if (p) dev_free(p, s);
+        p = nullptr;
+        n = 0;
+    }
+    T *get() const { return p; }
+};
+
+// ---------------------------------------------------------------- layout --
+// Device-resident FastLoad layout of one matrix.  The tile-ordered value and
+// row streams are the reference's sortval/sortrowidx (bit-identical); the
+// step table replaces the per-tile metadata for the streaming kernels.
+struct Regions;
+
+struct StepTable {
+    int steps = 0;              // h_count
+    DevBuf<int> col;            // first sorted column of step s
+    DevBuf<int> base;           // level of the step's first tile row
+    DevBuf<int> tall;           // levels in the step
+    DevBuf<int> tile_off;       // exclusive scan of tiles per step (steps+1)
+    DevBuf<int> nnz_off;        // exclusive scan of nonzeros per step (steps+1)
+};
+
+// Work items for the streaming SpMV kernels.  A region is the full-chunk
+// part or the partial-chunk part of one step; items cut regions into pieces
+// of at most FL_ITEM nonzeros whose interior boundaries sit on multiples of
+// four, so 128-bit loads stay aligned.
+struct RegionDesc {
+    int start;     // first nonzero of the region (stream position)
+    int col_base;  // first sorted column of the region
+    int div;       // 32*tall for a full region, len for a partial region
+    int full;      // 1: full 32-wide chunks, 0: the partial last chunk
+};
+struct ItemDesc {
+    int begin;     // first nonzero of the piece
+    int end;       // one past the last
+    int region;    // index into the region table
+    int pad;
+};
+
+struct Regions {
+    int nregions = 0;
+    int nitems = 0;
+    DevBuf<RegionDesc> region;
+    DevBuf<ItemDesc> item;
+};
+
+struct Layout {
+    int m = 0, n = 0, nnz = 0;
+    int tilenum = 0, segsum = 0;
+    StepTable st;
+    DevBuf<int> perm;           // sorted position -> original column
+    DevBuf<int> sortnnz;        // nnz per sorted column
+    // tile-ordered streams, padded to a multiple of FL_PAD entries
+    DevBuf<int> row;            // sortrowidx (-1 in the padding)
+    DevBuf<double> val;         // sortval (0 in the padding)
+    // reference per-tile arrays (kept for export and the tile kernel)
+    DevBuf<int> tile_ptr, tile_len, tile_colidx, tile_format;
+    DevBuf<int> sortrowindex;
+    DevBuf<int> countrow, segmentoffset;
+    Regions regions;
+};
+
+constexpr int FL_PAD = 512;     // stream padding granularity (entries)
+constexpr int FL_ITEM = 2048;   // nonzeros per work item of the stream kernel
+
+inline size_t padded(size_t n) { return ((n + FL_PAD - 1) / FL_PAD + 1) * FL_PAD; }
+
+// ---------------------------------------------------------- prep launchers --
+// Device-wide exclusive scan of n ints; out may alias in.  When total is
+// non-null the sum is written to total[0] (device memory).
+int scan_exclusive(const int *in, int *out, long n, int *total, cudaStream_t s);
+// Stable LSD radix sort of (key, value) pairs on the low `bits` bits.
+int radix_sort_pairs(unsigned *keys, unsigned *vals, long n, int bits, cudaStream_t s);
+int max_reduce(const int *in, long n, int *out_dev, cudaStream_t s);
+
+// CSR -> CSC transpose on the device (rows ascending per column).
+int csr_to_csc_device(int m, int n, int nnz, const int *rowptr, const int *colidx,
+                      const double *val, int *cscptr, int *cscrow, double *cscval,
+                      int *nnzpercol, cudaStream_t s);
+// Stable column sort; outputs are device arrays of the caller.
+int col_sort_device(int n, int nnz, const int *nnzpercol, const int *cscptr,
+                    const int *cscrow, const double *cscval, const double *x,
+                    int *perm, int *sortnnz, int *sortrowidx_tmp, double *sortval_tmp,
+                    double *sortx, cudaStream_t s);
+// Builds the full layout from column-sorted CSC arrays (device pointers).
+// with_reference_arrays: also build tile arrays, sortrowindex, countrow and
+// segmentoffset (needed by the reference export and the tile kernel).
+int build_layout_device(Layout &L, int m, int n, int nnz, const int *sortnnz,
+                        const int *sortrowidx_tmp, const double *sortval_tmp,
+                        bool with_reference_arrays, cudaStream_t s,
+                        float *ms_tran, float *ms_class);
+// Step table, tilenum and work items only (no payload): validates that
+// sortnnz is non-negative, ascending and sums to nnz.
+int build_steps(Layout &L, int m, int n, int nnz, const int *sortnnz, cudaStream_t s);
+int build_regions(Layout &L, cudaStream_t s);
+// Checks that host-provided per-tile arrays equal the ones the step table
+// implies (so the streaming kernels may derive columns arithmetically).
+int check_tile_meta(const Layout &L, const int *tile_ptr, const int *tile_len,
+                    const int *tile_colidx, cudaStream_t s);
+// cnt[c] = ptr[c+1] - ptr[c]
+int counts_from_ptr(const int *ptr, int n, int *cnt, cudaStream_t s);
+// FL_ERR_ARG unless every idx[i] is in [0, bound)
+int check_index_range(const int *idx, long count, int bound, const char *what,
+                      cudaStream_t s);
+// xs[i] = x[perm[i]]
+int permute_x(const int *perm, int n, const double *x, double *xs, cudaStream_t s);
+
+// ---------------------------------------------------------- spmv launchers --
+int spmv_stream_f64(const Layout &L, const double *xs, double *y, int variant,
+                    cudaStream_t s);
+int spmv_tile_f64(const Layout &L, const double *xs, double *y, cudaStream_t s);
+
+int num_sms();
+
+}  // namespace fl

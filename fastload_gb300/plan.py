@@ -1,0 +1,134 @@
+"""Device-resident FastLoad plans (fl_plan_* in include/fastload.h).
+
+A plan builds the FastLoad layout once on the GPU from device CSR/CSC arrays
+and keeps it in HBM; SpMV calls then run asynchronously on a CUDA stream.
+PyTorch tensors provide the device memory and the current stream.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from ._lib import PlanInfoC, SlideMatrixC, check, load
+from .host import SlideMatrix
+
+KERNEL_AUTO = 0
+KERNEL_TILE = 1
+KERNEL_STREAM = 2
+KERNEL_STREAM2 = 3
+
+
+def _torch():
+    import torch
+
+    return torch
+
+
+def _stream_handle(stream) -> C.c_void_p:
+    torch = _torch()
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return C.c_void_p(s.cuda_stream)
+
+
+def _dev(a, dtype):
+    """A contiguous CUDA tensor of dtype (uploads numpy input)."""
+    torch = _torch()
+    if isinstance(a, np.ndarray):
+        a = torch.from_numpy(np.ascontiguousarray(a))
+    t = a.to(device="cuda", dtype=dtype)
+    return t.contiguous()
+
+
+class Plan:
+    """FastLoad layout of one matrix resident on the current CUDA device."""
+
+    def __init__(self, handle: C.c_void_p, keep=None):
+        self._h = handle
+        self._keep = keep
+        self.info = self._info()
+        self.m, self.n, self.nnz = self.info["m"], self.info["n"], self.info["nnz"]
+
+    # -- construction ------------------------------------------------------
+    @classmethod
+    def from_csr(cls, m: int, n: int, rowptr, colidx, val, with_reference_arrays: bool = False, stream=None):
+        torch = _torch()
+        rp, ci, v = _dev(rowptr, torch.int32), _dev(colidx, torch.int32), _dev(val, torch.float64)
+        h = C.c_void_p()
+        check(load().fl_plan_create_csr(C.byref(h), m, n, int(ci.numel()), C.c_void_p(rp.data_ptr()),
+                                        C.c_void_p(ci.data_ptr()), C.c_void_p(v.data_ptr()),
+                                        int(with_reference_arrays), _stream_handle(stream)))
+        return cls(h)
+
+    @classmethod
+    def from_csc(cls, m: int, n: int, colptr, rowidx, val, with_reference_arrays: bool = False, stream=None):
+        torch = _torch()
+        cp, ri, v = _dev(colptr, torch.int32), _dev(rowidx, torch.int32), _dev(val, torch.float64)
+        h = C.c_void_p()
+        check(load().fl_plan_create_csc(C.byref(h), m, n, int(ri.numel()), C.c_void_p(cp.data_ptr()),
+                                        C.c_void_p(ri.data_ptr()), C.c_void_p(v.data_ptr()),
+                                        int(with_reference_arrays), _stream_handle(stream)))
+        return cls(h)
+
+    # -- queries -------------------------------------------------------------
+    def _info(self) -> dict:
+        i = PlanInfoC()
+        check(load().fl_plan_info_get(self._h, C.byref(i)))
+        return {k: getattr(i, k) for k, _ in PlanInfoC._fields_}
+
+    def export(self) -> tuple[SlideMatrix, np.ndarray]:
+        """The reference layout (host) and the column permutation."""
+        m = SlideMatrixC()
+        perm = np.empty(self.n, np.int32)
+        lib = load()
+        check(lib.fl_plan_export(self._h, C.byref(m), C.c_void_p(perm.ctypes.data)))
+        try:
+            sm = SlideMatrix._from_c(m, self.nnz)
+        finally:
+            lib.fl_tile_destroy(C.byref(m))
+        return sm, perm
+
+    # -- compute -------------------------------------------------------------
+    def permute_x(self, x, out=None, stream=None):
+        torch = _torch()
+        x = _dev(x, torch.float64)
+        xs = out if out is not None else torch.empty(self.n, dtype=torch.float64, device="cuda")
+        check(load().fl_plan_permute_x(self._h, C.c_void_p(x.data_ptr()), C.c_void_p(xs.data_ptr()),
+                                       _stream_handle(stream)))
+        return xs
+
+    def spmv(self, xs, y=None, accumulate: bool = False, kernel: int = KERNEL_AUTO, stream=None):
+        """y = A xs (or y += A xs); xs in sorted column order (permute_x)."""
+        torch = _torch()
+        if y is None:
+            y = torch.empty(self.m, dtype=torch.float64, device="cuda")
+            accumulate = False
+        check(load().fl_plan_spmv(self._h, C.c_void_p(xs.data_ptr()), C.c_void_p(y.data_ptr()), int(accumulate),
+                                  int(kernel), _stream_handle(stream)))
+        return y
+
+    def spmv_host(self, xs: np.ndarray, y: np.ndarray | None = None, kernel: int = KERNEL_AUTO, stream=None):
+        """Host buffers in and out: H2D of xs, SpMV, D2H of y (synchronous)."""
+        xs = np.ascontiguousarray(xs, dtype=np.float64)
+        if y is None:
+            y = np.empty(self.m, np.float64)
+        check(load().fl_plan_spmv_host(self._h, C.c_void_p(xs.ctypes.data), C.c_void_p(y.ctypes.data),
+                                       int(kernel), _stream_handle(stream)))
+        return y
+
+    def close(self) -> None:
+        if self._h:
+            load().fl_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()

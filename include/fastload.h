@@ -1,0 +1,177 @@
+/*
+ * fastload.h -- C ABI of the FastLoad GB300 CSC SpMV engine.
+ *
+ * Plain C: pointers, sizes and int status codes; no C++ or PyTorch types.
+ * Two groups of entry points:
+ *
+ *  1. Reference-compatible calls with HOST buffers that replace the calls
+ *     the reference's src/main.cu makes (csr_to_csc, ColSort,
+ *     formatTransform, FastLoad_spmv).  They are synchronous, produce the
+ *     reference's outputs bit for bit (layout) and fill the reference's
+ *     slide_matrix struct.  include/fastload_compat.h wraps them under the
+ *     reference's own names and C++ signatures.
+ *
+ *  2. A device-resident plan API: build the FastLoad layout once from device
+ *     CSR/CSC arrays, keep it in HBM and run y = A x on caller streams
+ *     (graph-capturable launches, no host round trips).
+ *
+ * Status codes are 0 on success and negative on failure; fl_last_error()
+ * returns the message of the last failure on the calling thread.  All
+ * indices are 32-bit, as in the reference (nnz < 2^31).
+ */
+#ifndef FASTLOAD_GB300_H
+#define FASTLOAD_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FL_SUCCESS 0
+#define FL_ERR_ARG (-1)       /* bad argument, malformed or inconsistent input */
+#define FL_ERR_CUDA (-2)      /* CUDA runtime error */
+#define FL_ERR_ALLOC (-3)     /* device or host allocation failed */
+#define FL_ERR_OVERFLOW (-4)  /* a count does not fit the 32-bit index space */
+#define FL_ERR_INTERNAL (-5)  /* internal consistency check failed */
+#define FL_ERR_NOT_READY (-6) /* bounded device wait expired */
+
+/* Same members, order and types as the reference's slide_matrix
+ * (src/format.h:6-20), so a pointer to either can be passed. */
+typedef struct fl_slide_matrix {
+    double *sortval;
+    int *sortrowidx;
+    int *tile_ptr;
+    int *tile_len;
+    int *tile_colidx;
+    int *tile_tall;
+    int *tile_format;
+    int *countrow;
+    int *segmentoffset;
+    int *sortrowindex;
+    int tilenum;
+    int segsum;
+} fl_slide_matrix;
+
+/* Message of the last failed call on this thread ("" if none). */
+const char *fl_last_error(void);
+/* Library version string. */
+const char *fl_version(void);
+/* Number of visible CUDA devices (0 when there is none). */
+int fl_device_count(void);
+
+/* ---- 1. reference-compatible host calls ------------------------------ */
+
+/* Replaces csr_to_csc (src/csr2csc_cuda.h:51-135; CPU twin
+ * src/coo2csc.h:11-72).  CSR (m x n) in, CSC out: rows ascending inside
+ * each column (CSR order for duplicate entries), csc_col_ptr has n+1
+ * entries, nnzpercol n.  *time_ms gets the device time of the transpose. */
+int fl_csr_to_csc(double *time_ms, int m, int n, int nnz, const double *csr_val,
+                  const int *csr_row_ptr, const int *csr_col_ind,
+                  double *csc_val, int *csc_row_ind, int *csc_col_ptr,
+                  int *nnzpercol);
+
+/* Replaces ColSort (src/ColSort_GPU.h:46-136).  Stable ascending sort of the
+ * columns by nonzero count (ties keep ascending column id, the order of
+ * thrust::sort_by_key at ColSort_GPU.h:101); writes the column-sorted CSC
+ * (sortrowidxTmp, sortvalTmp: nnz), the sorted counts (sortnnzTmp: colA) and
+ * the permuted x (sortx: colA).  Reads only colA entries of each per-column
+ * array. */
+int fl_col_sort(double *time_ms, int rowA, int colA, int nnz,
+                const int *nnzPerCol, const int *cscColPtr,
+                const int *cscRowIdx, const double *cscVal,
+                int *sortrowidxTmp, double *sortvalTmp, int *sortnnzTmp,
+                const double *x, double *sortx);
+
+/* Replaces formatTransform (src/formatTransform_GPU.h:289-596).  Builds the
+ * FastLoad tile layout from the column-sorted CSC and fills *matrix with
+ * malloc'd arrays the caller frees (fl_tile_destroy or the reference's
+ * Tile_destroy).  Unlike the reference's GPU path, every member is defined:
+ * tile_tall is zero-filled, countrow (tilenum+1), segmentoffset (segsum+1)
+ * and segsum are set as the reference's CPU path sets them
+ * (src/coo2csc.h:132-448).  *h_count gets the number of staircase steps. */
+int fl_format_transform(double *time_tran_ms, double *time_class_ms,
+                        fl_slide_matrix *matrix, const int *sortrowidx_tmp,
+                        const double *sortval_tmp, const int *sortnnz_tmp,
+                        int nnz, int rowA, int colA, int *h_count);
+
+/* Replaces FastLoad_spmv (src/FastLoad_GPU.h:275-409).  Uploads the layout
+ * and x_sorted, runs one untimed SpMV then `reps` timed ones (CUDA events,
+ * y zeroed before each), copies y = A x back (original row order) and, when
+ * y_golden is non-null, counts entries with |y_golden - y| > 0.01 |y|
+ * (the reference's check, FastLoad_GPU.h:383-389) into *mismatches.
+ * *ms_per_spmv gets the mean device time of one SpMV.  Any of the output
+ * pointers may be NULL. */
+int fl_fastload_spmv(const fl_slide_matrix *matrix, int nnz, int colA,
+                     int rowA, const double *x_sorted, double *y,
+                     const double *y_golden, int reps, double *ms_per_spmv,
+                     int *mismatches);
+
+/* Frees the arrays of a slide_matrix filled by fl_format_transform
+ * (src/format.h:29-42) and clears the pointers. */
+void fl_tile_destroy(fl_slide_matrix *matrix);
+
+/* ---- 2. device-resident plan API ------------------------------------- */
+
+typedef struct fl_plan *fl_plan_t;
+
+typedef struct fl_plan_info {
+    int m, n, nnz;
+    int tilenum;     /* tiles of the reference layout */
+    int steps;       /* staircase steps (h_count) */
+    int segsum;      /* runs of equal rows over all tiles */
+    int regions;     /* work regions of the streaming kernel */
+    int items;       /* work items of the streaming kernel */
+    size_t device_bytes; /* HBM held by the plan */
+} fl_plan_info;
+
+/* Builds a plan from a device CSR matrix (m x n).  stream may be NULL
+ * (legacy default stream).  Synchronises the stream once to size the
+ * layout.  with_reference_arrays != 0 also keeps the reference per-tile
+ * arrays on the device (needed by fl_plan_export and the tile kernel). */
+int fl_plan_create_csr(fl_plan_t *plan, int m, int n, int nnz,
+                       const int *d_rowptr, const int *d_colidx,
+                       const double *d_val, int with_reference_arrays,
+                       void *stream);
+/* Same from a device CSC matrix (rows ascending within each column). */
+int fl_plan_create_csc(fl_plan_t *plan, int m, int n, int nnz,
+                       const int *d_colptr, const int *d_rowidx,
+                       const double *d_val, int with_reference_arrays,
+                       void *stream);
+int fl_plan_info_get(fl_plan_t plan, fl_plan_info *info);
+/* Copies the reference layout into *matrix (malloc'd arrays, freed with
+ * fl_tile_destroy) and the column permutation into perm (n entries, may be
+ * NULL).  Needs a plan built with reference arrays. */
+int fl_plan_export(fl_plan_t plan, fl_slide_matrix *matrix, int *perm);
+/* xs[i] = x[perm[i]]: x in original column order -> sorted order. */
+int fl_plan_permute_x(fl_plan_t plan, const double *d_x, double *d_xs,
+                      void *stream);
+
+/* SpMV kernels of the plan (variant argument of fl_plan_spmv). */
+#define FL_KERNEL_AUTO 0     /* the default streaming kernel */
+#define FL_KERNEL_TILE 1     /* one warp per reference tile (reference-style) */
+#define FL_KERNEL_STREAM 2   /* streaming kernel, one block in flight per warp */
+#define FL_KERNEL_STREAM2 3  /* streaming kernel, two blocks in flight per warp */
+
+/* y = A xs (y zeroed first) or y += A xs when accumulate != 0; xs is in
+ * sorted column order (fl_plan_permute_x), y in original row order.
+ * Asynchronous on `stream`. */
+int fl_plan_spmv(fl_plan_t plan, const double *d_xs, double *d_y,
+                 int accumulate, int variant, void *stream);
+/* Host-buffer SpMV through the plan: copies xs (n doubles) to the device,
+ * runs y = A xs and copies y (m doubles) back; synchronous on `stream`.
+ * Pinned host buffers give the fastest copies. */
+int fl_plan_spmv_host(fl_plan_t plan, const double *h_xs, double *h_y,
+                      int variant, void *stream);
+int fl_plan_destroy(fl_plan_t plan);
+
+/* ---- test hooks ------------------------------------------------------- */
+
+/* Makes the `countdown`-th device allocation from now fail with
+ * FL_ERR_ALLOC (0 disables).  For error-path tests. */
+void fl_debug_fail_alloc_after(int countdown);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,94 @@
+/*
+ * fastload_compat.h -- the reference's host API names and C++ signatures
+ * over the C ABI of fastload.h, so a caller written against the reference
+ * (src/main.cu, test.cu) switches by replacing
+ *
+ *     #include "FastLoad_GPU.h" / "ColSort_GPU.h" /
+ *              "formatTransform_GPU.h" / "csr2csc_cuda.h"
+ *
+ * with `#include "fastload_compat.h"` and linking -lfastload_gb300.  Plain
+ * C++ (no CUDA headers): the caller compiles with g++.
+ *
+ * Like the reference, the shims return void and print errors; the int
+ * status and message stay available through the fl_* calls.
+ *
+ *   csr_to_csc      <- src/csr2csc_cuda.h:51-135
+ *   ColSort         <- src/ColSort_GPU.h:46-136
+ *   formatTransform <- src/formatTransform_GPU.h:289-596
+ *   FastLoad_spmv   <- src/FastLoad_GPU.h:275-409
+ *   Tile_destroy    <- src/format.h:29-42
+ */
+#ifndef FASTLOAD_GB300_COMPAT_H
+#define FASTLOAD_GB300_COMPAT_H
+
+#include <cstdio>
+
+#include "fastload.h"
+
+/* The reference's format.h defines slide_matrix and the slidesize macro
+ * (without an include guard).  When it is already included, use its type;
+ * otherwise define the same struct under the same name. */
+#ifndef slidesize
+typedef fl_slide_matrix slide_matrix;
+#define slidesize 32
+#define warpperblock 2
+#define FL_COMPAT_OWNS_SLIDE_MATRIX 1
+#endif
+
+static_assert(sizeof(slide_matrix) == sizeof(fl_slide_matrix), "slide_matrix layout differs from src/format.h");
+
+namespace fastload_compat_detail {
+inline void report(const char *who, int rc) {
+    if (rc != FL_SUCCESS) fprintf(stderr, "FastLoad GB300 %s error %d: %s\n", who, rc, fl_last_error());
+}
+}  // namespace fastload_compat_detail
+
+inline void csr_to_csc(double &time_csr2csc, int m, int n, int nnz, const double *csr_val,
+                       const int *csr_row_ptr, const int *csr_col_ind, double *csc_val, int *csc_row_ind,
+                       int *csc_col_ptr, int *nnzpercol) {
+    fastload_compat_detail::report("csr_to_csc",
+                                   fl_csr_to_csc(&time_csr2csc, m, n, nnz, csr_val, csr_row_ptr, csr_col_ind,
+                                                 csc_val, csc_row_ind, csc_col_ptr, nnzpercol));
+}
+
+inline void ColSort(double &timeForSort, int rowA, int colA, int nnz, int *nnzPerCol, int *cscColPtr,
+                    int *cscRowIdx, double *cscVal, int *sortrowidxTmp, double *sortvalTmp, int *sortnnzTmp,
+                    double *x, double *sortx) {
+    fastload_compat_detail::report("ColSort",
+                                   fl_col_sort(&timeForSort, rowA, colA, nnz, nnzPerCol, cscColPtr, cscRowIdx,
+                                               cscVal, sortrowidxTmp, sortvalTmp, sortnnzTmp, x, sortx));
+}
+
+inline void formatTransform(double &timeFormatTran, double &timeFormatclas, slide_matrix *matrix,
+                            int *sortrowidx_tmp, double *sortval_tmp, int *sortnnz_tmp, int nnz, int rowA,
+                            int colA, int &h_count) {
+    fastload_compat_detail::report(
+        "formatTransform", fl_format_transform(&timeFormatTran, &timeFormatclas, (fl_slide_matrix *)matrix,
+                                               sortrowidx_tmp, sortval_tmp, sortnnz_tmp, nnz, rowA, colA,
+                                               &h_count));
+}
+
+/* 100 timed SpMVs after one untimed run, y copied back, the reference's 1%
+ * check against y_golden and its result line (FastLoad_GPU.h:348-399). */
+inline void FastLoad_spmv(char *filename, slide_matrix *matrix, int nnz, int colA, int rowA, double *x,
+                          double *y, double *y_golden) {
+    (void)filename;
+    double ms = 0;
+    int bad = 0;
+    int rc = fl_fastload_spmv((const fl_slide_matrix *)matrix, nnz, colA, rowA, x, y, y_golden, 100, &ms, &bad);
+    if (rc != FL_SUCCESS) {
+        fastload_compat_detail::report("FastLoad_spmv", rc);
+        return;
+    }
+    double gflops = ms > 0 ? 2.0 * (double)nnz * 1.0e-6 / ms : 0.0;
+    if (bad == 0)
+        printf("Check FASTLOAD GPU PASS! (%f ms , %4.2f GFlops)\n", ms, gflops);
+    else
+        printf("Check NO PASS! error_count_slide_cuda = %d \n", bad);
+}
+
+#ifdef FL_COMPAT_OWNS_SLIDE_MATRIX
+inline void Tile_destroy(slide_matrix *matrix) { fl_tile_destroy(matrix); }
+#endif
+
+#endif

@@ -1,0 +1,179 @@
+"""CUDA path against the golden fixtures and the CPU oracle, through the C ABI.
+
+Layout (CSC, column sort, every slide_matrix array) must be bit-exact.  y
+must match the exactly rounded A x to a normwise relative error of 1e-12
+(the FP64 bound of the workload; atomics reorder the additions) and exactly
+when values and x are small integers, as in the reference's own check."""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import oracle
+from conftest import ROOT, golden_names, load_golden
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-12
+LAYOUT_KEYS = ["tile_ptr", "tile_len", "tile_colidx", "tile_tall", "tile_format", "countrow", "segmentoffset",
+               "sortrowindex", "sortrowidx", "sortval"]
+INTEGER_CASES = {"bus_i10", "spmv9", "runs", "dups"}
+KERNELS = ["KERNEL_AUTO", "KERNEL_STREAM", "KERNEL_STREAM2", "KERNEL_TILE"]
+
+
+def assert_y(y, g, name):
+    if name in INTEGER_CASES:
+        np.testing.assert_array_equal(y, g["y_exact"])
+    else:
+        nw, mx = oracle.rel_errors(y, g["y_exact"])
+        assert nw <= FP64_TOL and mx <= FP64_TOL, (name, nw, mx)
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_reference_calls_match_golden(gpu, name):
+    g = load_golden(name)
+    m, n, nnz = g["m"], g["n"], g["nnz"]
+    t, cv, cr, cp, cnt = gpu.csr_to_csc(m, n, nnz, g["val"], g["rowptr"], g["colidx"])
+    np.testing.assert_array_equal(cp, g["cscptr"])
+    np.testing.assert_array_equal(cr, g["cscrow"])
+    np.testing.assert_array_equal(cv, g["cscval"])
+    np.testing.assert_array_equal(cnt, g["nnzpercol"])
+    t, srow, sval, snnz, sx = gpu.ColSort(m, n, nnz, cnt, cp, cr, cv, g["x"])
+    np.testing.assert_array_equal(snnz, g["sortnnz"])
+    np.testing.assert_array_equal(sx, g["sortx"])
+    np.testing.assert_array_equal(srow, g["sortrowidx_tmp"])
+    np.testing.assert_array_equal(sval, g["sortval_tmp"])
+    ta, tb, sm, h = gpu.formatTransform(srow, sval, snnz, nnz, m, n)
+    assert sm.tilenum == g["tilenum"] and sm.segsum == g["segsum"]
+    for k in LAYOUT_KEYS:
+        np.testing.assert_array_equal(getattr(sm, k), g[k], err_msg=k)
+    y, ms, bad = gpu.FastLoad_spmv(sm, nnz, n, m, sx, y_golden=g["y_exact"], reps=3)
+    assert_y(y, g, name)
+    if name in INTEGER_CASES:
+        assert bad == 0
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_plan_matches_golden(gpu, name):
+    import torch
+
+    g = load_golden(name)
+    m, n = g["m"], g["n"]
+    with gpu.Plan.from_csr(m, n, g["rowptr"], g["colidx"], g["val"], with_reference_arrays=True) as p:
+        assert p.info["tilenum"] == g["tilenum"]
+        sm, perm = p.export()
+        np.testing.assert_array_equal(perm, g["perm"])
+        for k in LAYOUT_KEYS:
+            np.testing.assert_array_equal(getattr(sm, k), g[k], err_msg=k)
+        xs = p.permute_x(torch.from_numpy(g["x"]).cuda())
+        np.testing.assert_array_equal(xs.cpu().numpy(), g["sortx"])
+        for kern in KERNELS:
+            y = p.spmv(xs, kernel=getattr(gpu, kern))
+            torch.cuda.synchronize()
+            assert_y(y.cpu().numpy(), g, f"{name}/{kern}")
+        y2 = p.spmv_host(g["sortx"])
+        assert_y(y2, g, name)
+        # accumulate: y += A x on top of y = A x gives 2 A x
+        y = p.spmv(xs)
+        p.spmv(xs, y=y, accumulate=True)
+        assert_y(y.cpu().numpy() / 2, g, name)
+
+
+@pytest.mark.parametrize("name", ["cfg1", "bus_real", "zipf_small"])
+def test_plan_from_csc_matches_csr(gpu, name):
+    g = load_golden(name)
+    a = gpu.Plan.from_csr(g["m"], g["n"], g["rowptr"], g["colidx"], g["val"], with_reference_arrays=True)
+    b = gpu.Plan.from_csc(g["m"], g["n"], g["cscptr"], g["cscrow"], g["cscval"], with_reference_arrays=True)
+    sa, pa = a.export()
+    sb, pb = b.export()
+    np.testing.assert_array_equal(pa, pb)
+    for k in LAYOUT_KEYS:
+        np.testing.assert_array_equal(getattr(sa, k), getattr(sb, k))
+    a.close()
+    b.close()
+
+
+def test_fastload_spmv_accepts_the_reference_cpu_layout(gpu):
+    """A slide_matrix produced by the reference's own code (the golden) runs
+    through FastLoad_spmv unchanged."""
+    g = load_golden("cfg1")
+    sm = gpu.SlideMatrix(**{k: g[k] for k in LAYOUT_KEYS}, tilenum=int(g["tilenum"]), segsum=int(g["segsum"]))
+    y, ms, bad = gpu.FastLoad_spmv(sm, g["nnz"], g["n"], g["m"], g["sortx"], reps=2)
+    assert_y(y, g, "cfg1")
+
+
+def _full_size_case(kind):
+    from fastload_gb300 import gen
+
+    if kind == "zipf":
+        return gen.zipf_columns(1 << 20, 1.8, 50000, seed=2)
+    return gen.laplacian7(128, seed=4)
+
+
+@pytest.mark.parametrize("kind", ["zipf", "laplacian"])
+def test_full_size_layout_and_result(gpu, kind):
+    """Full benchmark sizes: the GPU layout equals the oracle's bit for bit;
+    y is within 1e-12 of the compensated oracle; linearity and the column-sum
+    checksum hold."""
+    import torch
+
+    c = _full_size_case(kind)
+    ref = oracle.build(c.m, c.n, csc=(c.colptr, c.rowidx, c.val), x=c.x)
+    with gpu.Plan.from_csc(c.m, c.n, c.colptr, c.rowidx, c.val, with_reference_arrays=True) as p:
+        sm, perm = p.export()
+        np.testing.assert_array_equal(perm, ref["perm"])
+        assert sm.tilenum == ref["tilenum"] and sm.segsum == ref["segsum"]
+        for k in LAYOUT_KEYS:
+            np.testing.assert_array_equal(getattr(sm, k), ref[k], err_msg=k)
+        x = torch.from_numpy(c.x).cuda()
+        xs = p.permute_x(x)
+        ydd = oracle.csc_spmv_dd(c.m, c.n, c.colptr, c.rowidx, c.val, c.x)
+        for kern in KERNELS:
+            y = p.spmv(xs, kernel=getattr(gpu, kern)).cpu().numpy()
+            nw, mx = oracle.rel_errors(y, ydd)
+            assert nw <= FP64_TOL and mx <= FP64_TOL, (kern, nw, mx)
+        # linearity: A(x1 + x2) = A x1 + A x2
+        x2 = torch.linspace(-1, 1, c.n, dtype=torch.float64, device="cuda")
+        xs2 = p.permute_x(x2)
+        ya = p.spmv(xs + xs2).cpu().numpy()
+        yb = (p.spmv(xs) + p.spmv(xs2)).cpu().numpy()
+        assert np.linalg.norm(ya - yb) <= 1e-12 * np.linalg.norm(ya)
+        # checksum: sum_i (A x)_i = sum_c x_c colsum_c
+        colsum = np.add.reduceat(c.val, c.colptr[:-1]) if c.nnz else np.zeros(c.n)
+        colsum[np.diff(c.colptr) == 0] = 0.0
+        y = p.spmv(xs).cpu().numpy()
+        assert abs(y.sum() - np.dot(colsum, c.x)) <= 1e-9 * np.abs(c.val).sum()
+
+
+def test_plan_build_is_deterministic(gpu):
+    g = load_golden("zipf_small")
+    outs = []
+    for _ in range(2):
+        with gpu.Plan.from_csr(g["m"], g["n"], g["rowptr"], g["colidx"], g["val"], with_reference_arrays=True) as p:
+            outs.append(p.export())
+    for k in LAYOUT_KEYS:
+        np.testing.assert_array_equal(getattr(outs[0][0], k), getattr(outs[1][0], k))
+
+
+def test_dropin_driver_runs_the_main_cu_sequence(gpu, tmp_path):
+    """tests/dropin/main_dropin.cpp (main.cu's call sequence on
+    fastload_compat.h) prints the reference's PASS line on 1138_bus."""
+    from fastload_gb300 import _build
+
+    exe = str(tmp_path / "dropin")
+    subprocess.run(["g++", "-O2", "-std=c++17", "-I", os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "dropin", "main_dropin.cpp"), "-o", exe,
+                    "-L", _build.LIBDIR, "-lfastload_gb300", f"-Wl,-rpath,{_build.LIBDIR}"], check=True)
+    g = load_golden("bus_i10")
+    path = tmp_path / "bus.bin"
+    with open(path, "wb") as f:
+        np.array([g["m"], g["n"], g["nnz"]], np.int32).tofile(f)
+        g["rowptr"].astype(np.int32).tofile(f)
+        g["colidx"].astype(np.int32).tofile(f)
+    r = subprocess.run([exe, str(path)], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "Check FASTLOAD GPU PASS!" in r.stdout
+    assert "Check FASTLOAD CPU PASS!" in r.stdout
+    assert f"tilenum {g['tilenum']}" in r.stdout
