@@ -25,12 +25,22 @@ def load_golden(name):
         return {k: (z[k].item() if z[k].ndim == 0 else z[k]) for k in z.files}
 
 
+def builder():
+    """fastload_gb300/_build.py loaded by path (importing the package needs
+    the built library)."""
+    import importlib.util
+
+    spec = importlib.util.spec_from_file_location("fastload_gb300_build",
+                                                  os.path.join(ROOT, "fastload_gb300", "_build.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
 @pytest.fixture(scope="session")
 def built_lib():
     """Builds (if stale) and loads the CUDA library; no GPU needed to load."""
-    from fastload_gb300 import _build
-
-    _build.build_library()
+    builder().build_library()
     from fastload_gb300 import _lib
 
     return _lib.load()
@@ -41,9 +51,7 @@ def gpu():
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
-    from fastload_gb300 import _build
-
-    _build.build_library()
+    builder().build_library()
     import fastload_gb300
 
     return fastload_gb300
