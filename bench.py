@@ -119,10 +119,14 @@ class ClockSampler:
                 "samples": len(rows)}
 
 
-def make_workload():
+def make_workload(n=N_COLS):
     from fastload_gb300 import gen
 
-    return gen.zipf_columns(N_COLS, 1.8, 50000, seed=SEED)
+    return gen.zipf_columns(n, 1.8, 50000, seed=SEED)
+
+
+def workload_name(n):
+    return WORKLOAD if n == N_COLS else f"fastload_fp64_zipf1.8_n{n}_cap50000"
 
 
 def cpu_baseline_sample(c, budget_s=12.0, threads=1):
@@ -155,7 +159,7 @@ def run_reference(args, rank, world):
         return
     import oracle
 
-    c = make_workload()
+    c = make_workload(args.n)
     lay = oracle.build(c.m, c.n, csc=(c.colptr, c.rowidx, c.val), x=c.x)
     T = int(lay["tilenum"])
     # each step: a bounded, rotating sample of about 1/16 of the tiles
@@ -185,7 +189,7 @@ def run_reference(args, rank, world):
     line = {"impl": "reference", "metric": METRIC, "value": gbs, "unit": "GB/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": DATA,
-            "config": {"workload": WORKLOAD, "n": c.n, "nnz": c.nnz, "seed": SEED},
+            "config": {"workload": workload_name(c.n), "n": c.n, "nnz": c.nnz, "seed": SEED},
             "cpu_baseline": {"value": gbs, "unit": "GB/s", "cores": used, "kind": "port",
                              "sample": f"{args.steps} steps, each 1/{nsamp} of the tiles in turn, FastLoad_cpu "
                                        f"tile loop on {used} OpenMP threads with atomic y updates"},
@@ -206,7 +210,7 @@ def run_gpu(args, rank, world):
         import torch.distributed as dist
 
         dist.init_process_group("nccl")
-    c = make_workload()
+    c = make_workload(args.n)
     m, n, nnz = c.m, c.n, c.nnz
     B = algorithmic_bytes(m, n, nnz)
     stream = torch.cuda.current_stream()
@@ -276,15 +280,16 @@ def run_gpu(args, rank, world):
             ts.append(a.elapsed_time(b))
         return float(np.mean(ts))
 
-    variants = {name: B / (time_kernel(k) * 1e-3) / 1e9 for name, k in
-                (("tile", fl.KERNEL_TILE), ("stream1", fl.KERNEL_STREAM), ("stream2", fl.KERNEL_STREAM2))}
+    variants = {} if args.quick else {
+        name: B / (time_kernel(k) * 1e-3) / 1e9 for name, k in
+        (("tile", fl.KERNEL_TILE), ("stream1", fl.KERNEL_STREAM), ("stream2", fl.KERNEL_STREAM2))}
 
     # end to end through the host-buffer C-ABI call: H2D of x, SpMV, D2H of y
     hx = torch.from_numpy(np.ascontiguousarray(plan.permute_x(x).cpu().numpy())).pin_memory().numpy()
     hy = torch.empty(m, dtype=torch.float64).pin_memory().numpy()
     for _ in range(3):
         plan.spmv_host(hx, hy, kernel=kernel)
-    ke = max(10, min(K, 200))
+    ke = 3 if args.quick else max(10, min(K, 200))
     t0 = time.perf_counter()
     for _ in range(ke):
         plan.spmv_host(hx, hy, kernel=kernel)
@@ -295,13 +300,13 @@ def run_gpu(args, rank, world):
         if dist:
             dist.destroy_process_group()
         return
-    cpu = cpu_baseline_sample(c) if world == 1 else None
-    traffic = ncu_traffic("k_spmv_stream_f64", WORKLOAD)
+    cpu = cpu_baseline_sample(c, budget_s=1.0 if args.quick else 12.0) if world == 1 else None
+    traffic = ncu_traffic("k_spmv_stream_f64", workload_name(n))
     line = {
         "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": K, "warmup": args.warmup,
         "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": DATA,
-        "config": {"workload": WORKLOAD, "m": m, "n": n, "nnz": nnz, "seed": SEED, "kernel": "stream (auto)",
+        "config": {"workload": workload_name(n), "m": m, "n": n, "nnz": nnz, "seed": SEED, "kernel": "stream (auto)",
                    "tilenum": plan.info["tilenum"], "steps_h_count": plan.info["steps"],
                    "l2": "inputs larger than L2: matrix streams %.0f MB vs 129 MB L2" % (nnz * 12 / 1e6),
                    "parallelism": f"replicas x{world}"},
@@ -332,6 +337,9 @@ def main():
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="fastload", choices=["fastload", "reference"])
+    ap.add_argument("--n", type=int, default=N_COLS, help="columns of the Zipf matrix (default 1,048,576)")
+    ap.add_argument("--quick", action="store_true", help="skip kernel variants, shorten e2e and CPU legs "
+                                                         "(for profiling runs)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", args.gpus if args.gpus == 1 else 1))
