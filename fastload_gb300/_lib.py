@@ -68,6 +68,7 @@ SIGNATURES = [
     ("fl_plan_spmv", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p]),
     ("fl_plan_spmv_host", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
     ("fl_plan_destroy", C.c_int, [C.c_void_p]),
+    ("fl_col_sort_noalloc", C.c_int, [C.c_int, C.c_int] + [C.c_void_p] * 11),
 ]
 
 _LIB = None

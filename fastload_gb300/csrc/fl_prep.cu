@@ -830,4 +830,141 @@ int build_regions(Layout &L, cudaStream_t s) {
     return FL_SUCCESS;
 }
 
+
+// ------------------------------------------------ allocation-free col sort --
+// A variant of the column sort for callers that cannot allocate device
+// memory at all -- for example a plugin inside a host application whose
+// allocator pre-reserves the whole device and refuses further requests, or
+// a latency-critical caller that cannot afford the synchronisation that
+// cudaMalloc/cudaFree imply.  Its scratch (radix-sort ping-pong buffers,
+// digit histograms, scan partial sums, the sorted column pointer and two
+// status words) lives in the file-scope array below, sized for at most
+// FL_NOALLOC_MAX_COLS columns; every GPU that loads this library holds it
+// until the process exits.  Host code must not pass the array's name to a
+// kernel (on the host it names a stand-in, not device memory): the first
+// call on each device looks up its device address with
+// cudaGetSymbolAddress while that device is current and caches it.
+namespace {
+constexpr long NA_COLS = FL_NOALLOC_MAX_COLS;
+constexpr long NA_TILES = (NA_COLS + RS_TILE - 1) / RS_TILE;
+constexpr long NA_HIST = RS_BINS * NA_TILES;
+constexpr long NA_SUMS = 2048;  // scan partial sums, two levels deep
+constexpr size_t NA_OFF_KEYS = 0;
+constexpr size_t NA_OFF_VALS = NA_OFF_KEYS + NA_COLS * sizeof(unsigned);
+constexpr size_t NA_OFF_HIST = NA_OFF_VALS + NA_COLS * sizeof(unsigned);
+constexpr size_t NA_OFF_SUMS = NA_OFF_HIST + NA_HIST * sizeof(int);
+constexpr size_t NA_OFF_COLPTR = NA_OFF_SUMS + NA_SUMS * sizeof(int);
+constexpr size_t NA_OFF_STATUS = NA_OFF_COLPTR + ((NA_COLS + 1 + 63) / 64) * 64 * sizeof(int);
+constexpr size_t NA_BYTES = NA_OFF_STATUS + 64;
+}  // namespace
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NA_BYTES];
+
+static std::mutex g_noalloc_mu;
+static unsigned char *g_noalloc_ptr[256];
+
+// Device address of the scratch array on the current device (set-up on the
+// first call per device).
+static int noalloc_scratch(unsigned char **out) {
+    int dev = 0;
+    FL_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 256) return fail(FL_ERR_INTERNAL, "device ordinal %d out of range", dev);
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p)
+            return fail(FL_ERR_CUDA, "cudaGetSymbolAddress(scratch) failed: %s", cudaGetErrorString(e));
+        g_noalloc_ptr[dev] = (unsigned char *)p;
+    }
+    *out = g_noalloc_ptr[dev];
+    return FL_SUCCESS;
+}
+
+// Exclusive scan whose partial sums go to caller scratch (sums, cap ints).
+static int scan_exclusive_into(const int *in, int *out, long n, int *total, int *sums, long cap, cudaStream_t s) {
+    if (n <= 0) {
+        if (total) FL_CUDA(cudaMemsetAsync(total, 0, sizeof(int), s));
+        return FL_SUCCESS;
+    }
+    long nb = (n + SCAN_TILE - 1) / SCAN_TILE;
+    if (nb == 1) {
+        k_scan_apply<<<1, SCAN_THREADS, 0, s>>>(in, out, n, nullptr, total);
+        FL_CUDA(cudaGetLastError());
+        return FL_SUCCESS;
+    }
+    if (nb > cap) return fail(FL_ERR_INTERNAL, "scan scratch too small (%ld > %ld)", nb, cap);
+    k_scan_reduce<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(in, n, sums);
+    FL_CUDA(cudaGetLastError());
+    FL_TRY(scan_exclusive_into(sums, sums, nb, nullptr, sums + nb, cap - nb, s));
+    k_scan_apply<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(in, out, n, sums, total);
+    FL_CUDA(cudaGetLastError());
+    return FL_SUCCESS;
+}
+
+extern "C" int fl_col_sort_noalloc(int n, int nnz, const int *d_nnzpercol, const int *d_colptr,
+                                   const int *d_rowidx, const double *d_val, const double *d_x, int *d_perm,
+                                   int *d_sortnnz, int *d_sortrowidx_tmp, double *d_sortval_tmp, double *d_sortx,
+                                   void *stream) {
+    clear_error();
+    cudaStream_t s = (cudaStream_t)stream;
+    if (n < 0 || nnz < 0) return fail(FL_ERR_ARG, "col_sort_noalloc: negative size (n=%d nnz=%d)", n, nnz);
+    if (n > FL_NOALLOC_MAX_COLS)
+        return fail(FL_ERR_ARG, "col_sort_noalloc: n=%d exceeds FL_NOALLOC_MAX_COLS=%d (the scratch array size); "
+                                "use fl_col_sort or a plan for larger matrices", n, FL_NOALLOC_MAX_COLS);
+    if (n == 0) {
+        if (nnz != 0) return fail(FL_ERR_ARG, "col_sort_noalloc: nnz=%d with no columns", nnz);
+        return FL_SUCCESS;
+    }
+    if (!d_nnzpercol || !d_colptr || !d_perm || !d_sortnnz || (d_x && !d_sortx) ||
+        (nnz && (!d_rowidx || !d_val || !d_sortrowidx_tmp || !d_sortval_tmp)))
+        return fail(FL_ERR_ARG, "col_sort_noalloc: NULL array");
+    unsigned char *base = nullptr;
+    FL_TRY(noalloc_scratch(&base));
+    unsigned *k2 = (unsigned *)(base + NA_OFF_KEYS), *v2 = (unsigned *)(base + NA_OFF_VALS);
+    int *hist = (int *)(base + NA_OFF_HIST), *sums = (int *)(base + NA_OFF_SUMS);
+    int *scolptr = (int *)(base + NA_OFF_COLPTR), *status = (int *)(base + NA_OFF_STATUS);
+    // status words start at zero on every call (the array keeps the last
+    // call's contents)
+    FL_CUDA(cudaMemsetAsync(status, 0, 2 * sizeof(int), s));
+    k_validate_counts<<<grid_for(n, 256), 256, 0, s>>>(d_nnzpercol, d_colptr, n, nnz, status);
+    FL_CUDA(cudaGetLastError());
+    k_max<<<grid_for(n, 256), 256, 0, s>>>(d_nnzpercol, n, status + 1);
+    FL_CUDA(cudaGetLastError());
+    int h[2] = {0, 0};
+    FL_CUDA(cudaMemcpyAsync(h, status, sizeof h, cudaMemcpyDeviceToHost, s));
+    FL_CUDA(cudaStreamSynchronize(s));
+    if (h[0]) return fail(FL_ERR_ARG, "col_sort_noalloc: inconsistent input (flags 0x%x: 1=negative count, "
+                                      "2=count disagrees with colptr, 4=colptr[0]!=0 or colptr[n]!=nnz)", h[0]);
+    unsigned *ki = (unsigned *)d_sortnnz, *vi = (unsigned *)d_perm, *ko = k2, *vo = v2;
+    FL_CUDA(cudaMemcpyAsync(ki, d_nnzpercol, (size_t)n * sizeof(int), cudaMemcpyDeviceToDevice, s));
+    k_iota<<<grid_for(n, 256), 256, 0, s>>>(vi, n);
+    FL_CUDA(cudaGetLastError());
+    const long ntiles = (n + RS_TILE - 1) / RS_TILE;
+    for (int shift = 0; shift < bits_for((unsigned long)h[1]); shift += 8) {
+        k_radix_hist<<<(unsigned)ntiles, RS_THREADS, 0, s>>>(ki, n, shift, hist, (int)ntiles);
+        FL_CUDA(cudaGetLastError());
+        FL_TRY(scan_exclusive_into(hist, hist, ntiles * RS_BINS, nullptr, sums, NA_SUMS, s));
+        k_radix_scatter<<<(unsigned)ntiles, RS_THREADS, 0, s>>>(ki, vi, ko, vo, n, shift, hist, (int)ntiles);
+        FL_CUDA(cudaGetLastError());
+        std::swap(ki, ko);
+        std::swap(vi, vo);
+    }
+    if (ki != (unsigned *)d_sortnnz) {
+        FL_CUDA(cudaMemcpyAsync(d_sortnnz, ki, (size_t)n * sizeof(int), cudaMemcpyDeviceToDevice, s));
+        FL_CUDA(cudaMemcpyAsync(d_perm, vi, (size_t)n * sizeof(int), cudaMemcpyDeviceToDevice, s));
+    }
+    if (d_x) {
+        k_gather_x<<<grid_for(n, 256), 256, 0, s>>>((const unsigned *)d_perm, n, d_x, d_sortx);
+        FL_CUDA(cudaGetLastError());
+    }
+    if (nnz > 0) {
+        FL_TRY(scan_exclusive_into(d_sortnnz, scolptr, n, scolptr + n, sums, NA_SUMS, s));
+        k_sorted_gather<<<grid_for(nnz, 256), 256, 0, s>>>(d_perm, scolptr, n, nnz, d_colptr, d_rowidx, d_val,
+                                                           d_sortrowidx_tmp, d_sortval_tmp);
+        FL_CUDA(cudaGetLastError());
+    }
+    return FL_SUCCESS;
+}
+
 }  // namespace fl

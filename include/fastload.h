@@ -165,6 +165,43 @@ int fl_plan_spmv_host(fl_plan_t plan, const double *h_xs, double *h_y,
                       int variant, void *stream);
 int fl_plan_destroy(fl_plan_t plan);
 
+/* ---- allocation-free column sort -------------------------------------- */
+
+/* Largest column count fl_col_sort_noalloc accepts (its scratch array holds
+ * about 3.3 MB of device memory for this many columns). */
+#define FL_NOALLOC_MAX_COLS 262144
+
+/* No counterpart in the reference: an extra entry point for callers that
+ * cannot allocate device memory -- for example a plugin whose host
+ * application has already reserved the whole GPU in its own pool and refuses
+ * further allocations, or a latency-critical caller that cannot afford the
+ * device-wide synchronisation cudaMalloc/cudaFree bring.  It computes what
+ * fl_col_sort computes (stable sort of the columns by nonzero count, the
+ * column-sorted CSC and the permuted x) but on DEVICE arrays the caller
+ * provides, and it calls no cudaMalloc, cudaFree or other allocating
+ * routine.  Its scratch is one statically sized device array in the library,
+ * present on every GPU that loads the library until the process exits.
+ *
+ *  - n must be at most FL_NOALLOC_MAX_COLS; larger n returns FL_ERR_ARG
+ *    with a message (use fl_col_sort or a plan instead).
+ *  - The first call on a device looks up the scratch array's device address
+ *    (with that device current); make that first call before any stream
+ *    capture.
+ *  - All calls share the one scratch array, which keeps the last call's
+ *    contents (the entry point zeroes what must start at zero).  Calls that
+ *    overlap on the GPU -- on different streams or from different host
+ *    threads -- race on it; serialise them.
+ *  - Synchronises `stream` once (to read the validation result); the rest is
+ *    asynchronous on `stream` (NULL = legacy default stream).
+ * Inputs: d_nnzpercol (n), d_colptr (n+1), d_rowidx, d_val (nnz), d_x (n,
+ * may be NULL).  Outputs: d_perm, d_sortnnz (n), d_sortrowidx_tmp,
+ * d_sortval_tmp (nnz), d_sortx (n, when d_x is given). */
+int fl_col_sort_noalloc(int n, int nnz, const int *d_nnzpercol,
+                        const int *d_colptr, const int *d_rowidx,
+                        const double *d_val, const double *d_x, int *d_perm,
+                        int *d_sortnnz, int *d_sortrowidx_tmp,
+                        double *d_sortval_tmp, double *d_sortx, void *stream);
+
 /* ---- test hooks ------------------------------------------------------- */
 
 /* Makes the `countdown`-th device allocation from now fail with
