@@ -280,9 +280,10 @@ def run_gpu(args, rank, world):
             ts.append(a.elapsed_time(b))
         return float(np.mean(ts))
 
-    variants = {} if args.quick else {
-        name: B / (time_kernel(k) * 1e-3) / 1e9 for name, k in
-        (("tile", fl.KERNEL_TILE), ("stream1", fl.KERNEL_STREAM), ("stream2", fl.KERNEL_STREAM2))}
+    kernels = [("tile", fl.KERNEL_TILE), ("stream1", fl.KERNEL_STREAM), ("stream2", fl.KERNEL_STREAM2)]
+    if plan.info["heavy_cols"]:
+        kernels.append(("bucket", fl.KERNEL_BUCKET))
+    variants = {} if args.quick else {name: B / (time_kernel(k) * 1e-3) / 1e9 for name, k in kernels}
 
     # end to end through the host-buffer C-ABI call: H2D of x, SpMV, D2H of y
     hx = torch.from_numpy(np.ascontiguousarray(plan.permute_x(x).cpu().numpy())).pin_memory().numpy()
@@ -301,12 +302,16 @@ def run_gpu(args, rank, world):
             dist.destroy_process_group()
         return
     cpu = cpu_baseline_sample(c, budget_s=1.0 if args.quick else 12.0) if world == 1 else None
-    traffic = ncu_traffic("k_spmv_stream_f64", workload_name(n))
+    kname = "k_spmv_bucket_f64" if plan.info["heavy_cols"] else "k_spmv_stream_f64"
+    traffic = ncu_traffic(kname, workload_name(n))
+    plan.check()
     line = {
         "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": K, "warmup": args.warmup,
         "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": DATA,
-        "config": {"workload": workload_name(n), "m": m, "n": n, "nnz": nnz, "seed": SEED, "kernel": "stream (auto)",
+        "config": {"workload": workload_name(n), "m": m, "n": n, "nnz": nnz, "seed": SEED,
+                   "kernel": "bucketed (auto)" if plan.info["heavy_cols"] else "stream (auto)",
+                   "heavy_band_cols": plan.info["heavy_cols"], "heavy_band_nnz": plan.info["heavy_nnz"],
                    "tilenum": plan.info["tilenum"], "steps_h_count": plan.info["steps"],
                    "l2": "inputs larger than L2: matrix streams %.0f MB vs 129 MB L2" % (nnz * 12 / 1e6),
                    "parallelism": f"replicas x{world}"},
@@ -314,10 +319,11 @@ def run_gpu(args, rank, world):
         "gflops": 2.0 * nnz * world / (ms_step * 1e-3) / 1e9,
         "rel_err_vs_fp64_oracle": {"normwise": rel[0], "max_over_inf": rel[1]},
         "kernel_variants_gbs": variants,
+        "speedup_vs_plain_fp64_stream": (variants["stream2"] and achieved / variants["stream2"]) if variants else None,
         "preprocess_s": prep_s,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_kind": f"{peak_kind} hbm_gbs",
-                     "kernel": "k_spmv_stream_f64", "bytes_per_launch": B, "kernel_ms": kern_ms},
+                     "kernel": kname, "bytes_per_launch": B, "kernel_ms": kern_ms},
         "cpu_baseline": cpu,
         "e2e": {"value": B / e2e_s / 1e9, "unit": "GB/s", "h2d_bytes_per_step": n * 8, "d2h_bytes_per_step": m * 8,
                 "ms_per_step": e2e_s * 1e3, "call": "fl_plan_spmv_host (pinned host x and y)",

@@ -7,11 +7,12 @@ ImportError when that library is missing.
 """
 from ._lib import FastLoadError, load
 from .host import ColSort, FastLoad_spmv, SlideMatrix, csr_to_csc, formatTransform
-from .plan import KERNEL_AUTO, KERNEL_STREAM, KERNEL_STREAM2, KERNEL_TILE, Plan
+from .plan import INPUT_CSC, INPUT_CSR, KERNEL_AUTO, KERNEL_BUCKET, KERNEL_STREAM, KERNEL_STREAM2, KERNEL_TILE, Plan
 
 load()
 
 __all__ = [
     "FastLoadError", "SlideMatrix", "csr_to_csc", "ColSort", "formatTransform", "FastLoad_spmv", "Plan",
-    "KERNEL_AUTO", "KERNEL_TILE", "KERNEL_STREAM", "KERNEL_STREAM2", "load",
+    "KERNEL_AUTO", "KERNEL_TILE", "KERNEL_STREAM", "KERNEL_STREAM2", "KERNEL_BUCKET", "INPUT_CSR", "INPUT_CSC",
+    "load",
 ]

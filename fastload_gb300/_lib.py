@@ -39,7 +39,12 @@ class PlanInfoC(C.Structure):
     _fields_ = [
         ("m", C.c_int), ("n", C.c_int), ("nnz", C.c_int), ("tilenum", C.c_int), ("steps", C.c_int),
         ("segsum", C.c_int), ("regions", C.c_int), ("items", C.c_int), ("device_bytes", C.c_size_t),
+        ("heavy_cols", C.c_int), ("heavy_nnz", C.c_int), ("heavy_slices", C.c_int), ("heavy_padded", C.c_int),
     ]
+
+
+class PlanOptsC(C.Structure):
+    _fields_ = [("with_reference_arrays", C.c_int), ("heavy_band", C.c_int), ("reserved", C.c_int * 6)]
 
 
 # (name, restype, argtypes) of every exported symbol; tests check the .so
@@ -58,6 +63,10 @@ SIGNATURES = [
     ("fl_fastload_spmv", C.c_int, [C.POINTER(SlideMatrixC), C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
                                    C.c_void_p, C.c_int, c_double_p, c_int_p]),
     ("fl_tile_destroy", None, [C.POINTER(SlideMatrixC)]),
+    ("fl_plan_create", C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p,
+                                 C.c_void_p, C.c_void_p, C.POINTER(PlanOptsC), C.c_void_p]),
+    ("fl_plan_max_heavy_band", C.c_int, []),
+    ("fl_plan_check", C.c_int, [C.c_void_p]),
     ("fl_plan_create_csr", C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
                                      C.c_void_p, C.c_int, C.c_void_p]),
     ("fl_plan_create_csc", C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p,

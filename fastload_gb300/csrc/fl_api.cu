@@ -8,6 +8,7 @@
 
 #include <cstdlib>
 #include <cstring>
+#include <memory>
 #include <new>
 
 namespace fl {
@@ -20,6 +21,7 @@ using namespace fl;
 struct fl_plan {
     Layout L;
     bool has_ref = false;
+    std::unique_ptr<Bucket> bucket;    // bucketed form (heavy band), optional
     DevBuf<double> stage_x, stage_y;  // device staging of fl_plan_spmv_host
 };
 
@@ -361,62 +363,87 @@ void fl_tile_destroy(fl_slide_matrix *m) {
 
 // ------------------------------------------------------------ plan API --
 static int plan_from_csc(fl_plan_t *out, int m, int n, int nnz, const int *colptr, const int *rowidx,
-                         const double *val, int with_ref, cudaStream_t s) {
-    fl_plan *p = new (std::nothrow) fl_plan();
+                         const double *val, const fl_plan_opts &o, cudaStream_t s) {
+    std::unique_ptr<fl_plan> p(new (std::nothrow) fl_plan());
     if (!p) return fail(FL_ERR_ALLOC, "plan: host allocation failed");
-    DevBuf<int> cnt, snnz, srow;
+    DevBuf<int> cnt, srow;
     DevBuf<double> sval;
-    int rc = FL_SUCCESS;
-    auto bail = [&](int code) {
-        delete p;
-        return code;
-    };
-    if ((rc = cnt.alloc(n, s))) return bail(rc);
-    if ((rc = p->L.perm.alloc(n, s))) return bail(rc);
-    if ((rc = p->L.sortnnz.alloc(n, s))) return bail(rc);
-    if ((rc = srow.alloc(nnz, s))) return bail(rc);
-    if ((rc = sval.alloc(nnz, s))) return bail(rc);
-    if ((rc = counts_from_ptr(colptr, n, cnt.get(), s))) return bail(rc);
-    if ((rc = col_sort_device(n, nnz, cnt.get(), colptr, rowidx, val, nullptr, p->L.perm.get(), p->L.sortnnz.get(),
-                              srow.get(), sval.get(), nullptr, s)))
-        return bail(rc);
-    if ((rc = build_layout_device(p->L, m, n, nnz, p->L.sortnnz.get(), srow.get(), sval.get(), with_ref != 0, s,
-                                  nullptr, nullptr)))
-        return bail(rc);
-    p->has_ref = with_ref != 0;
+    FL_TRY(cnt.alloc(n, s));
+    FL_TRY(p->L.perm.alloc(n, s));
+    FL_TRY(p->L.sortnnz.alloc(n, s));
+    FL_TRY(srow.alloc(nnz, s));
+    FL_TRY(sval.alloc(nnz, s));
+    FL_TRY(counts_from_ptr(colptr, n, cnt.get(), s));
+    FL_TRY(col_sort_device(n, nnz, cnt.get(), colptr, rowidx, val, nullptr, p->L.perm.get(), p->L.sortnnz.get(),
+                           srow.get(), sval.get(), nullptr, s));
+    FL_TRY(build_layout_device(p->L, m, n, nnz, p->L.sortnnz.get(), srow.get(), sval.get(),
+                               o.with_reference_arrays != 0, s, nullptr, nullptr));
+    p->has_ref = o.with_reference_arrays != 0;
+    if (o.heavy_band >= 0) {
+        int nh = o.heavy_band;
+        if (nh == 0) {
+            nh = bucket_auto_band(p->L.sortnnz.get(), n, nnz, s);
+            if (nh < 0) return nh;
+        } else if (nh > bucket_max_band() || nh > n) {
+            return fail(FL_ERR_ARG, "plan: heavy_band=%d exceeds min(n=%d, %d)", nh, n, bucket_max_band());
+        }
+        if (nh > 0) {
+            p->bucket.reset(new (std::nothrow) Bucket());
+            if (!p->bucket) return fail(FL_ERR_ALLOC, "plan: host allocation failed");
+            FL_TRY(build_bucket(*p->bucket, m, n, nnz, p->L.sortnnz.get(), srow.get(), sval.get(), nh, s));
+        }
+    }
     cudaError_t e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess) return bail(fail(FL_ERR_CUDA, "plan: %s", cudaGetErrorString(e)));
-    *out = p;
+    if (e != cudaSuccess) return fail(FL_ERR_CUDA, "plan: %s", cudaGetErrorString(e));
+    *out = p.release();
     return FL_SUCCESS;
 }
 
-int fl_plan_create_csc(fl_plan_t *plan, int m, int n, int nnz, const int *d_colptr, const int *d_rowidx,
-                       const double *d_val, int with_reference_arrays, void *stream) {
-    clear_error();
-    if (!plan) return fail(FL_ERR_ARG, "plan_create_csc: NULL plan pointer");
-    *plan = nullptr;
-    FL_TRY(check_sizes("plan_create_csc", m, n, nnz));
-    if (!d_colptr || (nnz && (!d_rowidx || !d_val))) return fail(FL_ERR_ARG, "plan_create_csc: NULL array");
-    FL_TRY(check_index_range(d_rowidx, nnz, m, "plan_create_csc: row index", (cudaStream_t)stream));
-    return plan_from_csc(plan, m, n, nnz, d_colptr, d_rowidx, d_val, with_reference_arrays, (cudaStream_t)stream);
+static fl_plan_opts default_opts(int with_ref) {
+    fl_plan_opts o;
+    memset(&o, 0, sizeof o);
+    o.with_reference_arrays = with_ref;
+    return o;
 }
 
-int fl_plan_create_csr(fl_plan_t *plan, int m, int n, int nnz, const int *d_rowptr, const int *d_colidx,
-                       const double *d_val, int with_reference_arrays, void *stream) {
+int fl_plan_max_heavy_band(void) { return bucket_max_band(); }
+
+int fl_plan_create(fl_plan_t *plan, int input_format, int m, int n, int nnz, const int *d_ptr, const int *d_idx,
+                   const double *d_val, const fl_plan_opts *opts, void *stream) {
     clear_error();
-    if (!plan) return fail(FL_ERR_ARG, "plan_create_csr: NULL plan pointer");
+    if (!plan) return fail(FL_ERR_ARG, "plan_create: NULL plan pointer");
     *plan = nullptr;
-    FL_TRY(check_sizes("plan_create_csr", m, n, nnz));
-    if (!d_rowptr || (nnz && (!d_colidx || !d_val))) return fail(FL_ERR_ARG, "plan_create_csr: NULL array");
+    FL_TRY(check_sizes("plan_create", m, n, nnz));
+    if (!d_ptr || (nnz && (!d_idx || !d_val))) return fail(FL_ERR_ARG, "plan_create: NULL array");
+    if (input_format != FL_INPUT_CSR && input_format != FL_INPUT_CSC)
+        return fail(FL_ERR_ARG, "plan_create: unknown input format %d", input_format);
+    const fl_plan_opts o = opts ? *opts : default_opts(0);
+    if (o.heavy_band < -1) return fail(FL_ERR_ARG, "plan_create: heavy_band=%d", o.heavy_band);
     cudaStream_t s = (cudaStream_t)stream;
+    if (input_format == FL_INPUT_CSC) {
+        FL_TRY(check_index_range(d_idx, nnz, m, "plan_create: row index", s));
+        return plan_from_csc(plan, m, n, nnz, d_ptr, d_idx, d_val, o, s);
+    }
     DevBuf<int> cp, cr, npc;
     DevBuf<double> cv;
     FL_TRY(cp.alloc((size_t)n + 1, s));
     FL_TRY(cr.alloc(nnz, s));
     FL_TRY(cv.alloc(nnz, s));
     FL_TRY(npc.alloc(n, s));
-    FL_TRY(csr_to_csc_device(m, n, nnz, d_rowptr, d_colidx, d_val, cp.get(), cr.get(), cv.get(), npc.get(), s));
-    return plan_from_csc(plan, m, n, nnz, cp.get(), cr.get(), cv.get(), with_reference_arrays, s);
+    FL_TRY(csr_to_csc_device(m, n, nnz, d_ptr, d_idx, d_val, cp.get(), cr.get(), cv.get(), npc.get(), s));
+    return plan_from_csc(plan, m, n, nnz, cp.get(), cr.get(), cv.get(), o, s);
+}
+
+int fl_plan_create_csc(fl_plan_t *plan, int m, int n, int nnz, const int *d_colptr, const int *d_rowidx,
+                       const double *d_val, int with_reference_arrays, void *stream) {
+    const fl_plan_opts o = default_opts(with_reference_arrays);
+    return fl_plan_create(plan, FL_INPUT_CSC, m, n, nnz, d_colptr, d_rowidx, d_val, &o, stream);
+}
+
+int fl_plan_create_csr(fl_plan_t *plan, int m, int n, int nnz, const int *d_rowptr, const int *d_colidx,
+                       const double *d_val, int with_reference_arrays, void *stream) {
+    const fl_plan_opts o = default_opts(with_reference_arrays);
+    return fl_plan_create(plan, FL_INPUT_CSR, m, n, nnz, d_rowptr, d_colidx, d_val, &o, stream);
 }
 
 int fl_plan_info_get(fl_plan_t p, fl_plan_info *info) {
@@ -435,6 +462,22 @@ int fl_plan_info_get(fl_plan_t p, fl_plan_info *info) {
                L.tile_colidx.n * 4 + L.tile_format.n * 4 + L.sortrowindex.n * 4 + L.countrow.n * 4 +
                L.segmentoffset.n * 4 + L.regions.region.n * sizeof(RegionDesc) +
                L.regions.item.n * sizeof(ItemDesc) + 5 * (size_t)(L.st.steps + 1) * 4;
+    info->heavy_cols = 0;
+    info->heavy_nnz = 0;
+    info->heavy_slices = 0;
+    info->heavy_padded = 0;
+    if (p->bucket) {
+        const Bucket &B = *p->bucket;
+        const HeavyBand &H = B.heavy;
+        info->heavy_cols = H.nh;
+        info->heavy_nnz = (int)H.nnz;
+        info->heavy_slices = H.nslices;
+        info->heavy_padded = (int)H.padded;
+        const Layout &Q = B.light;
+        b += Q.row.n * 4 + Q.val.n * 8 + Q.regions.region.n * sizeof(RegionDesc) +
+             Q.regions.item.n * sizeof(ItemDesc) + 5 * (size_t)(Q.st.steps + 1) * 4;
+        b += H.val.n * 8 + H.col.n * 2 + H.slice_ptr.n * 4 + H.row.n * 4 + H.len.n * 4;
+    }
     info->device_bytes = b;
     return FL_SUCCESS;
 }
@@ -464,6 +507,11 @@ int fl_plan_spmv(fl_plan_t p, const double *d_xs, double *d_y, int accumulate, i
     if (!accumulate && p->L.m) FL_CUDA(cudaMemsetAsync(d_y, 0, (size_t)p->L.m * sizeof(double), s));
     switch (variant) {
         case FL_KERNEL_AUTO:
+            if (p->bucket) return spmv_bucket_f64(*p->bucket, d_xs, d_y, s);
+            return spmv_stream_f64(p->L, d_xs, d_y, FL_KERNEL_STREAM2, s);
+        case FL_KERNEL_BUCKET:
+            if (!p->bucket) return fail(FL_ERR_ARG, "plan_spmv: the plan has no heavy band");
+            return spmv_bucket_f64(*p->bucket, d_xs, d_y, s);
         case FL_KERNEL_STREAM:
         case FL_KERNEL_STREAM2: return spmv_stream_f64(p->L, d_xs, d_y, variant, s);
         case FL_KERNEL_TILE: return spmv_tile_f64(p->L, d_xs, d_y, s);
@@ -482,6 +530,18 @@ int fl_plan_spmv_host(fl_plan_t p, const double *h_xs, double *h_y, int variant,
     FL_TRY(fl_plan_spmv(p, p->stage_x.get(), p->stage_y.get(), 0, variant, stream));
     FL_TRY(download(h_y, p->stage_y.get(), p->L.m, s));
     FL_CUDA(cudaStreamSynchronize(s));
+    return FL_SUCCESS;
+}
+
+int fl_plan_check(fl_plan_t p) {
+    clear_error();
+    if (!p) return fail(FL_ERR_ARG, "plan_check: NULL plan");
+    FL_CUDA(cudaDeviceSynchronize());
+    if (!p->bucket) return FL_SUCCESS;
+    int h = 0;
+    FL_CUDA(cudaMemcpy(&h, p->bucket->err.get(), sizeof(int), cudaMemcpyDeviceToHost));
+    FL_CUDA(cudaMemset(p->bucket->err.get(), 0, sizeof(int)));
+    if (h) return fail(FL_ERR_NOT_READY, "bucket kernel: staging of the heavy band's x did not complete (0x%x)", h);
     return FL_SUCCESS;
 }
 

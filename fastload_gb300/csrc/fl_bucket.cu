@@ -1,0 +1,368 @@
+// fl_bucket.cu -- bucketed FastLoad SpMV (FP64) for sm_103a.
+//
+// The column sort of FastLoad orders columns by nonzero count; a bucket
+// threshold H0 splits that order in two:
+//
+//  * light columns [0, H0) keep the FastLoad layout (tiles of the staircase
+//    restricted to those columns) and the streaming kernel's per-run atomics;
+//  * the heavy band [H0, n) -- the densest columns, which on skewed matrices
+//    hold most of the nonzeros -- is re-packed row-major into slices of 32
+//    rows: lane l of a slice owns one row and walks its band nonzeros,
+//    accumulating value * x with one FP64 FMA each, x read from shared
+//    memory (the band's x is staged there by a TMA bulk copy at kernel start,
+//    overlapped with the light work), and adds the row's sum to y with one
+//    atomic.
+//
+// On GB300 scattered L2 atomics (about 221 G/s) and FP64 pipe slots (about
+// 500 G/s) are the scarce resources of a CSC SpMV; the heavy band turns one
+// atomic per nonzero into one per row and keeps exactly one FP64 operation
+// per nonzero.  One persistent launch runs both parts.
+#include "fl_stream.cuh"
+
+#include <algorithm>
+#include <vector>
+
+namespace fl {
+
+constexpr int BK_THREADS = 1024;
+constexpr int BK_MAX_BAND = 24576;            // 192 KB of FP64 x in shared memory
+constexpr int BK_AUTO_BAND = 16384;           // default band width cap
+constexpr int BK_AUTO_MIN_DEGREE = 32;        // densest columns worth a row slice
+constexpr long BK_WAIT_LIMIT = 1L << 20;      // bounded mbarrier polling
+constexpr int HV_UNROLL = 4;                  // heavy-slice loads in flight per lane
+
+int bucket_max_band() { return BK_MAX_BAND; }
+
+static int grid_cap(long n, int threads, int per_sm = 8) {
+    long b = (n + threads - 1) / threads;
+    long cap = (long)num_sms() * per_sm;
+    return (int)std::max<long>(1, std::min(b, cap));
+}
+
+// ------------------------------------------------------------- build ----
+__global__ void k_band_ptr(const int *scolptr, int H0, int nh, int *bandptr) {
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i <= nh; i += (long)gridDim.x * blockDim.x)
+        bandptr[i] = scolptr[H0 + i] - scolptr[H0];
+}
+
+// key = maxlen - len (so an ascending stable sort lists rows longest first,
+// ties in ascending row id); counts rows with band nonzeros.
+__global__ void k_len_key(const int *rlen, int m, int maxlen, unsigned *key, unsigned *idx, int *nrows) {
+    int c = 0;
+    for (long r = blockIdx.x * (long)blockDim.x + threadIdx.x; r < m; r += (long)gridDim.x * blockDim.x) {
+        int l = rlen[r];
+        key[r] = (unsigned)(maxlen - l);
+        idx[r] = (unsigned)r;
+        c += l > 0;
+    }
+    for (int o = 16; o; o >>= 1) c += __shfl_xor_sync(FULLM, c, o);
+    if ((threadIdx.x & 31) == 0 && c) atomicAdd(nrows, c);
+}
+
+__global__ void k_slice_width(const unsigned *rows, const int *rlen, int nslices, int *width32) {
+    for (long s = blockIdx.x * (long)blockDim.x + threadIdx.x; s < nslices; s += (long)gridDim.x * blockDim.x)
+        width32[s] = 32 * rlen[rows[32 * s]];
+}
+
+// One warp per slice: lane l copies row rows[32s+l]'s band entries to
+// slice_ptr[s] + 32 j + l (zero padding past the row's length).
+__global__ void k_slice_fill(const unsigned *rows, const int *rlen, const int *rp, const int *hc,
+                             const double *hv, int nrows, int nslices, const int *slice_ptr, double *val,
+                             uint16_t *col, int *srow, int *slen) {
+    const int lane = threadIdx.x & 31;
+    long gw = (blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5, nw = ((long)gridDim.x * blockDim.x) >> 5;
+    for (long s = gw; s < nslices; s += nw) {
+        const long slot = 32 * s + lane;
+        const int r = slot < nrows ? (int)rows[slot] : -1;
+        const int len = r >= 0 ? rlen[r] : 0;
+        srow[slot] = r;
+        slen[slot] = len;
+        const int base = slice_ptr[s], w = (slice_ptr[s + 1] - base) >> 5;
+        const int src = r >= 0 ? rp[r] : 0;
+        for (int j = 0; j < w; j++) {
+            const long dst = base + 32L * j + lane;
+            val[dst] = j < len ? hv[src + j] : 0.0;
+            col[dst] = j < len ? (uint16_t)hc[src + j] : (uint16_t)0;
+        }
+    }
+}
+
+static int read_ints(cudaStream_t s, const int *dev, int *host, int count) {
+    FL_CUDA(cudaMemcpyAsync(host, dev, count * sizeof(int), cudaMemcpyDeviceToHost, s));
+    FL_CUDA(cudaStreamSynchronize(s));
+    return FL_SUCCESS;
+}
+
+static int bits_of(unsigned long v) {
+    int b = 0;
+    while (v) { b++; v >>= 1; }
+    return b;
+}
+
+int bucket_auto_band(const int *sortnnz, int n, int nnz, cudaStream_t s) {
+    if (n <= 0 || nnz <= 0) return 0;
+    const int tail = std::min(n, BK_AUTO_BAND);
+    std::vector<int> h(tail);
+    FL_TRY(read_ints(s, sortnnz + (n - tail), h.data(), tail));
+    int band = 0;
+    long band_nnz = 0;
+    for (int i = tail - 1; i >= 0 && h[i] >= BK_AUTO_MIN_DEGREE; i--) {
+        band++;
+        band_nnz += h[i];
+    }
+    band &= ~1;
+    // a band worth its own pass holds a quarter of the matrix or more
+    if (band < 64 || band_nnz * 4 < (long)nnz) return 0;
+    return band;
+}
+
+int build_bucket(Bucket &B, int m, int n, int nnz, const int *sortnnz, const int *srow_tmp,
+                 const double *sval_tmp, int nh, cudaStream_t s) {
+    nh = std::max(0, std::min(nh, std::min(n, BK_MAX_BAND))) & ~1;
+    const int H0 = n - nh;
+    DevBuf<int> scolptr;
+    FL_TRY(scolptr.alloc((size_t)n + 1, s));
+    FL_TRY(scan_exclusive(sortnnz, scolptr.get(), n, scolptr.get() + n, s));
+    int nnz_l = 0;
+    FL_TRY(read_ints(s, scolptr.get() + H0, &nnz_l, 1));
+    FL_TRY(build_layout_device(B.light, m, H0, nnz_l, sortnnz, srow_tmp, sval_tmp, false, s, nullptr, nullptr));
+    HeavyBand &H = B.heavy;
+    H.H0 = H0;
+    H.nh = nh;
+    H.nnz = (long)nnz - nnz_l;
+    FL_TRY(B.err.alloc(1, s));
+    FL_CUDA(cudaMemsetAsync(B.err.get(), 0, sizeof(int), s));
+    FL_TRY(B.next.alloc(1, s));
+    if (nh == 0 || H.nnz == 0) {
+        H.nh = 0;
+        return FL_SUCCESS;
+    }
+    const int nnz_h = (int)H.nnz;
+    // band as CSR over the matrix rows (local columns ascending in each row)
+    DevBuf<int> bandptr, rp, hc, rlen, scal;
+    DevBuf<double> hv;
+    FL_TRY(bandptr.alloc((size_t)nh + 1, s));
+    k_band_ptr<<<grid_cap(nh + 1, 256), 256, 0, s>>>(scolptr.get(), H0, nh, bandptr.get());
+    FL_CUDA(cudaGetLastError());
+    FL_TRY(rp.alloc((size_t)m + 1, s));
+    FL_TRY(hc.alloc(nnz_h, s));
+    FL_TRY(hv.alloc(nnz_h, s));
+    FL_TRY(rlen.alloc(std::max(m, 1), s));
+    FL_TRY(csr_to_csc_device(nh, m, nnz_h, bandptr.get(), srow_tmp + nnz_l, sval_tmp + nnz_l, rp.get(), hc.get(),
+                             hv.get(), rlen.get(), s));
+    // rows longest first
+    FL_TRY(scal.alloc(2, s));
+    FL_CUDA(cudaMemsetAsync(scal.get(), 0, 2 * sizeof(int), s));
+    FL_TRY(max_reduce(rlen.get(), m, scal.get(), s));
+    int h2[2];
+    FL_TRY(read_ints(s, scal.get(), h2, 1));
+    const int maxlen = h2[0];
+    DevBuf<unsigned> keys, rows;
+    FL_TRY(keys.alloc(m, s));
+    FL_TRY(rows.alloc(m, s));
+    k_len_key<<<grid_cap(m, 256), 256, 0, s>>>(rlen.get(), m, maxlen, keys.get(), rows.get(), scal.get() + 1);
+    FL_CUDA(cudaGetLastError());
+    FL_TRY(radix_sort_pairs(keys.get(), rows.get(), m, bits_of((unsigned long)maxlen), s));
+    FL_TRY(read_ints(s, scal.get(), h2, 2));
+    H.nrows = h2[1];
+    H.nslices = (H.nrows + 31) / 32;
+    FL_TRY(H.slice_ptr.alloc((size_t)H.nslices + 1, s));
+    DevBuf<int> width32;
+    FL_TRY(width32.alloc((size_t)H.nslices + 1, s));
+    k_slice_width<<<grid_cap(H.nslices, 256), 256, 0, s>>>(rows.get(), rlen.get(), H.nslices, width32.get());
+    FL_CUDA(cudaGetLastError());
+    FL_TRY(scan_exclusive(width32.get(), H.slice_ptr.get(), H.nslices, H.slice_ptr.get() + H.nslices, s));
+    int total = 0;
+    FL_TRY(read_ints(s, H.slice_ptr.get() + H.nslices, &total, 1));
+    H.padded = total;
+    FL_TRY(H.val.alloc(std::max(total, 1), s));
+    FL_TRY(H.col.alloc(std::max(total, 1), s));
+    FL_TRY(H.row.alloc(32L * H.nslices, s));
+    FL_TRY(H.len.alloc(32L * H.nslices, s));
+    k_slice_fill<<<grid_cap(32L * H.nslices, 256, 16), 256, 0, s>>>(
+        rows.get(), rlen.get(), rp.get(), hc.get(), hv.get(), H.nrows, H.nslices, H.slice_ptr.get(), H.val.get(),
+        H.col.get(), H.row.get(), H.len.get());
+    FL_CUDA(cudaGetLastError());
+    FL_CUDA(cudaStreamSynchronize(s));
+    return FL_SUCCESS;
+}
+
+// ------------------------------------------------------------ kernel ----
+struct BucketArgs {
+    // light part
+    const ItemDesc *items;
+    const RegionDesc *regions;
+    const int *row;
+    const double *val;
+    int nitems;
+    // heavy band
+    int H0, nh, nslices, bulk;
+    const int *slice_ptr, *hrow, *hlen;
+    const double *hval;
+    const uint16_t *hcol;
+    const double *xs;
+    double *y;
+    int *err;
+    int *next;  // work counter: units [0, nitems) are light items, then heavy slices
+};
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t phase) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(phase)
+        : "memory");
+    return ok != 0;
+}
+
+__device__ __forceinline__ double ld_stream_f64(const double *p) {
+    double r;
+    asm("ld.global.nc.L1::no_allocate.f64 %0, [%1];" : "=d"(r) : "l"(p));
+    return r;
+}
+__device__ __forceinline__ unsigned short ld_stream_u16(const uint16_t *p) {
+    unsigned short r;
+    asm("ld.global.nc.L1::no_allocate.u16 %0, [%1];" : "=h"(r) : "l"(p));
+    return r;
+}
+
+template <int U>
+__global__ void __launch_bounds__(BK_THREADS, 1) k_spmv_bucket_f64(const BucketArgs a) {
+    extern __shared__ __align__(128) double xh[];
+    __shared__ __align__(8) unsigned long long mbar;
+    const int tid = threadIdx.x, lane = tid & 31;
+    const int gw = (blockIdx.x * blockDim.x + tid) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t bar = smem_addr(&mbar);
+    if (a.nh > 0) {
+        if (a.bulk) {
+            if (tid == 0) {
+                asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+                asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+            }
+            __syncthreads();
+            if (tid == 0) {
+                const uint32_t bytes = (uint32_t)a.nh * 8u;
+                asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+                             : "memory");
+                const char *src = (const char *)(a.xs + a.H0);
+                const uint32_t dst = smem_addr(xh);
+                for (uint32_t off = 0; off < bytes; off += 32768u) {
+                    const uint32_t sz = min(32768u, bytes - off);
+                    asm volatile(
+                        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+                            "r"(dst + off),
+                        "l"(src + off), "r"(sz), "r"(bar)
+                        : "memory");
+                }
+            }
+        } else {
+            for (int i = tid; i < a.nh; i += blockDim.x) xh[i] = __ldg(a.xs + a.H0 + i);
+            __syncthreads();
+        }
+    }
+    // Work units are handed out by a counter: light items first (the band's
+    // x arrives meanwhile), then heavy slices widest first, so every warp
+    // keeps busy until the last unit.
+    const int total = a.nitems + (a.nh > 0 ? a.nslices : 0);
+    bool staged = !(a.nh > 0 && a.bulk);
+    for (;;) {
+        int u = 0;
+        if (lane == 0) u = atomicAdd(a.next, 1);
+        u = __shfl_sync(FULLM, u, 0);
+        if (u >= total) break;
+        if (u < a.nitems) {
+            stream_item_f64<U>(a.items[u], a.regions, a.row, a.val, a.xs, a.y, lane);
+            continue;
+        }
+        if (!staged) {
+            bool ok = false;
+            for (long i = 0; i < BK_WAIT_LIMIT && !ok; i++) ok = mbar_try_wait(bar, 0);
+            if (!ok) {
+                if (lane == 0) atomicOr(a.err, 1);
+                break;
+            }
+            staged = true;
+        }
+        // heavy slice: one lane per row
+        const int sl = u - a.nitems;
+        const int base = __ldg(a.slice_ptr + sl);
+        const int w = (__ldg(a.slice_ptr + sl + 1) - base) >> 5;
+        const int r = __ldg(a.hrow + 32 * sl + lane), len = __ldg(a.hlen + 32 * sl + lane);
+        const double *vp = a.hval + base + lane;
+        const uint16_t *cp = a.hcol + base + lane;
+        double acc = 0.0;
+        int j = 0;
+        for (; j + HV_UNROLL <= w; j += HV_UNROLL) {
+            double v[HV_UNROLL];
+            unsigned short c[HV_UNROLL];
+#pragma unroll
+            for (int k = 0; k < HV_UNROLL; k++) {
+                if (j + k < len) {
+                    v[k] = ld_stream_f64(vp + 32 * (j + k));
+                    c[k] = ld_stream_u16(cp + 32 * (j + k));
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < HV_UNROLL; k++)
+                if (j + k < len) acc = fma(v[k], xh[c[k]], acc);
+        }
+        for (; j < w; j++)
+            if (j < len) acc = fma(ld_stream_f64(vp + 32 * j), xh[ld_stream_u16(cp + 32 * j)], acc);
+        if (len > 0) atomicAdd(a.y + r, acc);
+    }
+    // a block must not exit while its bulk copy may still write its shared
+    // memory: wait (bounded) when no warp of this block waited yet
+    if (a.nh > 0 && a.bulk && !staged) {
+        bool ok = false;
+        for (long i = 0; i < BK_WAIT_LIMIT && !ok; i++) ok = mbar_try_wait(bar, 0);
+        if (!ok && lane == 0) atomicOr(a.err, 2);
+    }
+}
+
+int spmv_bucket_f64(const Bucket &B, const double *xs, double *y, cudaStream_t s) {
+    const HeavyBand &H = B.heavy;
+    const Regions &R = B.light.regions;
+    static bool attr_set = false;
+    if (!attr_set) {
+        FL_CUDA(cudaFuncSetAttribute(k_spmv_bucket_f64<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     BK_MAX_BAND * (int)sizeof(double)));
+        attr_set = true;
+    }
+    BucketArgs a;
+    a.items = R.item.get();
+    a.regions = R.region.get();
+    a.row = B.light.row.get();
+    a.val = B.light.val.get();
+    a.nitems = R.nitems;
+    a.H0 = H.H0;
+    a.nh = H.nnz > 0 ? H.nh : 0;
+    a.nslices = H.nslices;
+    a.slice_ptr = H.slice_ptr.get();
+    a.hrow = H.row.get();
+    a.hlen = H.len.get();
+    a.hval = H.val.get();
+    a.hcol = H.col.get();
+    a.xs = xs;
+    a.y = y;
+    a.err = B.err.get();
+    a.next = B.next.get();
+    const size_t bytes = (size_t)a.nh * sizeof(double);
+    a.bulk = a.nh > 0 && ((uintptr_t)(xs + H.H0) % 16 == 0) && bytes % 16 == 0;
+    if (a.nitems == 0 && a.nslices == 0) return FL_SUCCESS;
+    FL_CUDA(cudaMemsetAsync(a.next, 0, sizeof(int), s));
+    int per_sm = 0;
+    FL_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_spmv_bucket_f64<2>, BK_THREADS, bytes));
+    if (per_sm <= 0) per_sm = 1;
+    const long warps_needed = (long)a.nitems + a.nslices;
+    const long grid = std::max<long>(1, std::min<long>((long)num_sms() * per_sm, (warps_needed + 31) / 32));
+    k_spmv_bucket_f64<2><<<(int)grid, BK_THREADS, bytes, s>>>(a);
+    FL_CUDA(cudaGetLastError());
+    return FL_SUCCESS;
+}
+
+}  // namespace fl

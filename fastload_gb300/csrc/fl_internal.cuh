@@ -123,6 +123,32 @@ struct Layout {
     Regions regions;
 };
 
+// Heavy band of the bucketed form: the nh densest sorted columns, stored as
+// slices of 32 rows (rows sorted by their band nonzero count, longest
+// first); slice s holds width_s entries per lane, entry j of lane l at
+// slice_ptr[s] + 32*j + l.  Columns are local (sorted column - H0) so they
+// fit 16 bits and index the band's x staged in shared memory.
+struct HeavyBand {
+    int H0 = 0, nh = 0;         // first sorted column of the band, its width
+    int nslices = 0, nrows = 0; // slices; rows with band nonzeros
+    long nnz = 0;               // band nonzeros (no padding)
+    long padded = 0;            // slice entries including padding
+    DevBuf<double> val;
+    DevBuf<uint16_t> col;
+    DevBuf<int> slice_ptr;      // nslices+1
+    DevBuf<int> row;            // 32*nslices, -1 for an empty lane
+    DevBuf<int> len;            // 32*nslices
+};
+
+// Bucketed form: light columns [0, H0) keep the FastLoad tile stream, the
+// heavy band [H0, n) uses row slices.
+struct Bucket {
+    Layout light;
+    HeavyBand heavy;
+    DevBuf<int> err;            // device status word of the bucket kernel
+    DevBuf<int> next;           // work counter of the bucket kernel (zeroed per launch)
+};
+
 constexpr int FL_PAD = 512;     // stream padding granularity (entries)
 constexpr int FL_ITEM = 2048;   // nonzeros per work item of the stream kernel
 
@@ -172,6 +198,16 @@ int permute_x(const int *perm, int n, const double *x, double *xs, cudaStream_t 
 int spmv_stream_f64(const Layout &L, const double *xs, double *y, int variant,
                     cudaStream_t s);
 int spmv_tile_f64(const Layout &L, const double *xs, double *y, cudaStream_t s);
+// Bucketed form: build from the column-sorted CSC (device) and run.
+int build_bucket(Bucket &B, int m, int n, int nnz, const int *sortnnz, const int *srow_tmp,
+                 const double *sval_tmp, int nh, cudaStream_t s);
+int spmv_bucket_f64(const Bucket &B, const double *xs, double *y, cudaStream_t s);
+// Largest heavy band the bucket kernel can stage in shared memory.
+int bucket_max_band();
+// Heavy band width chosen from the sorted column counts (device array):
+// the densest columns with at least `min_degree` nonzeros, at most the
+// shared-memory limit, or 0 when the band would hold little of the matrix.
+int bucket_auto_band(const int *sortnnz, int n, int nnz, cudaStream_t s);
 
 int num_sms();
 

@@ -10,13 +10,16 @@ import ctypes as C
 
 import numpy as np
 
-from ._lib import PlanInfoC, SlideMatrixC, check, load
+from ._lib import PlanInfoC, PlanOptsC, SlideMatrixC, check, load
 from .host import SlideMatrix
 
 KERNEL_AUTO = 0
 KERNEL_TILE = 1
 KERNEL_STREAM = 2
 KERNEL_STREAM2 = 3
+KERNEL_BUCKET = 4
+INPUT_CSR = 0
+INPUT_CSC = 1
 
 
 def _torch():
@@ -51,24 +54,29 @@ class Plan:
 
     # -- construction ------------------------------------------------------
     @classmethod
-    def from_csr(cls, m: int, n: int, rowptr, colidx, val, with_reference_arrays: bool = False, stream=None):
+    def create(cls, input_format: int, m: int, n: int, ptr, idx, val, with_reference_arrays: bool = False,
+               heavy_band: int = 0, stream=None):
+        """input_format INPUT_CSR (ptr = row pointer) or INPUT_CSC (ptr =
+        column pointer).  heavy_band: -1 no bucketed form, 0 automatic, > 0
+        width of the heavy band in columns."""
         torch = _torch()
-        rp, ci, v = _dev(rowptr, torch.int32), _dev(colidx, torch.int32), _dev(val, torch.float64)
+        p, i, v = _dev(ptr, torch.int32), _dev(idx, torch.int32), _dev(val, torch.float64)
+        o = PlanOptsC(int(with_reference_arrays), int(heavy_band))
         h = C.c_void_p()
-        check(load().fl_plan_create_csr(C.byref(h), m, n, int(ci.numel()), C.c_void_p(rp.data_ptr()),
-                                        C.c_void_p(ci.data_ptr()), C.c_void_p(v.data_ptr()),
-                                        int(with_reference_arrays), _stream_handle(stream)))
+        check(load().fl_plan_create(C.byref(h), int(input_format), m, n, int(i.numel()), C.c_void_p(p.data_ptr()),
+                                    C.c_void_p(i.data_ptr()), C.c_void_p(v.data_ptr()), C.byref(o),
+                                    _stream_handle(stream)))
         return cls(h)
 
     @classmethod
-    def from_csc(cls, m: int, n: int, colptr, rowidx, val, with_reference_arrays: bool = False, stream=None):
-        torch = _torch()
-        cp, ri, v = _dev(colptr, torch.int32), _dev(rowidx, torch.int32), _dev(val, torch.float64)
-        h = C.c_void_p()
-        check(load().fl_plan_create_csc(C.byref(h), m, n, int(ri.numel()), C.c_void_p(cp.data_ptr()),
-                                        C.c_void_p(ri.data_ptr()), C.c_void_p(v.data_ptr()),
-                                        int(with_reference_arrays), _stream_handle(stream)))
-        return cls(h)
+    def from_csr(cls, m: int, n: int, rowptr, colidx, val, with_reference_arrays: bool = False,
+                 heavy_band: int = 0, stream=None):
+        return cls.create(INPUT_CSR, m, n, rowptr, colidx, val, with_reference_arrays, heavy_band, stream)
+
+    @classmethod
+    def from_csc(cls, m: int, n: int, colptr, rowidx, val, with_reference_arrays: bool = False,
+                 heavy_band: int = 0, stream=None):
+        return cls.create(INPUT_CSC, m, n, colptr, rowidx, val, with_reference_arrays, heavy_band, stream)
 
     # -- queries -------------------------------------------------------------
     def _info(self) -> dict:
@@ -115,6 +123,11 @@ class Plan:
         check(load().fl_plan_spmv_host(self._h, C.c_void_p(xs.ctypes.data), C.c_void_p(y.ctypes.data),
                                        int(kernel), _stream_handle(stream)))
         return y
+
+    def check(self) -> None:
+        """Raises FastLoadError if a bounded device wait of the plan's
+        kernels expired since the last check (synchronises the device)."""
+        check(load().fl_plan_check(self._h))
 
     def close(self) -> None:
         if self._h:

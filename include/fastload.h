@@ -123,12 +123,40 @@ typedef struct fl_plan_info {
     int regions;     /* work regions of the streaming kernel */
     int items;       /* work items of the streaming kernel */
     size_t device_bytes; /* HBM held by the plan */
+    int heavy_cols;  /* bucketed form: width of the heavy band (0: none) */
+    int heavy_nnz;   /* nonzeros in the heavy band */
+    int heavy_slices;/* 32-row slices of the heavy band */
+    int heavy_padded;/* slice entries including padding */
 } fl_plan_info;
 
-/* Builds a plan from a device CSR matrix (m x n).  stream may be NULL
- * (legacy default stream).  Synchronises the stream once to size the
- * layout.  with_reference_arrays != 0 also keeps the reference per-tile
- * arrays on the device (needed by fl_plan_export and the tile kernel). */
+/* Plan build options (NULL = defaults: no reference arrays, automatic
+ * heavy band). */
+typedef struct fl_plan_opts {
+    int with_reference_arrays; /* keep the reference per-tile arrays */
+    int heavy_band;  /* bucketed form: -1 off, 0 automatic (the densest
+                        columns with >= 32 nonzeros, at most 16384, when they
+                        hold >= 1/4 of the matrix), > 0 that many of the
+                        densest columns (even, at most fl_plan_max_heavy_band()) */
+    int reserved[6];
+} fl_plan_opts;
+
+#define FL_INPUT_CSR 0
+#define FL_INPUT_CSC 1
+
+/* Builds a plan from a device CSR (input_format FL_INPUT_CSR: ptr = row
+ * pointer m+1, idx = column indices) or CSC (FL_INPUT_CSC: ptr = column
+ * pointer n+1, idx = row indices, rows ascending per column) matrix. */
+int fl_plan_create(fl_plan_t *plan, int input_format, int m, int n, int nnz,
+                   const int *d_ptr, const int *d_idx, const double *d_val,
+                   const fl_plan_opts *opts, void *stream);
+/* Widest heavy band the bucketed kernel can stage in shared memory. */
+int fl_plan_max_heavy_band(void);
+
+/* Builds a plan from a device CSR matrix (m x n) with the default heavy
+ * band.  stream may be NULL (legacy default stream).  Synchronises the
+ * stream a few times to size the layout.  with_reference_arrays != 0 also
+ * keeps the reference per-tile arrays on the device (needed by
+ * fl_plan_export and the tile kernel). */
 int fl_plan_create_csr(fl_plan_t *plan, int m, int n, int nnz,
                        const int *d_rowptr, const int *d_colidx,
                        const double *d_val, int with_reference_arrays,
@@ -148,10 +176,11 @@ int fl_plan_permute_x(fl_plan_t plan, const double *d_x, double *d_xs,
                       void *stream);
 
 /* SpMV kernels of the plan (variant argument of fl_plan_spmv). */
-#define FL_KERNEL_AUTO 0     /* the default streaming kernel */
+#define FL_KERNEL_AUTO 0     /* bucketed kernel when the plan has a heavy band, else streaming */
 #define FL_KERNEL_TILE 1     /* one warp per reference tile (reference-style) */
 #define FL_KERNEL_STREAM 2   /* streaming kernel, one block in flight per warp */
 #define FL_KERNEL_STREAM2 3  /* streaming kernel, two blocks in flight per warp */
+#define FL_KERNEL_BUCKET 4   /* light columns streamed + heavy band in row slices */
 
 /* y = A xs (y zeroed first) or y += A xs when accumulate != 0; xs is in
  * sorted column order (fl_plan_permute_x), y in original row order.
@@ -164,6 +193,9 @@ int fl_plan_spmv(fl_plan_t plan, const double *d_xs, double *d_y,
 int fl_plan_spmv_host(fl_plan_t plan, const double *h_xs, double *h_y,
                       int variant, void *stream);
 int fl_plan_destroy(fl_plan_t plan);
+/* Reads and clears the device status word of the plan's kernels (0 when no
+ * bounded wait expired); synchronises the device. */
+int fl_plan_check(fl_plan_t plan);
 
 /* ---- allocation-free column sort -------------------------------------- */
 
