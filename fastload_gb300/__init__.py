@@ -7,12 +7,13 @@ ImportError when that library is missing.
 """
 from ._lib import FastLoadError, load
 from .host import ColSort, FastLoad_spmv, SlideMatrix, csr_to_csc, formatTransform
-from .plan import INPUT_CSC, INPUT_CSR, KERNEL_AUTO, KERNEL_BUCKET, KERNEL_STREAM, KERNEL_STREAM2, KERNEL_TILE, Plan
+from .plan import (BAND_ALL, BAND_AUTO, BAND_NONE, INPUT_CSC, INPUT_CSR, KERNEL_AUTO, KERNEL_BUCKET, KERNEL_STREAM,
+                   KERNEL_STREAM2, KERNEL_TILE, VALUES_BF16X2, VALUES_F32, VALUES_F64, Plan)
 
 load()
 
 __all__ = [
     "FastLoadError", "SlideMatrix", "csr_to_csc", "ColSort", "formatTransform", "FastLoad_spmv", "Plan",
     "KERNEL_AUTO", "KERNEL_TILE", "KERNEL_STREAM", "KERNEL_STREAM2", "KERNEL_BUCKET", "INPUT_CSR", "INPUT_CSC",
-    "load",
+    "VALUES_F64", "VALUES_F32", "VALUES_BF16X2", "BAND_AUTO", "BAND_NONE", "BAND_ALL", "load",
 ]

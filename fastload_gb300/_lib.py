@@ -43,6 +43,11 @@ class PlanInfoC(C.Structure):
     ]
 
 
+class FormInfoC(C.Structure):
+    _fields_ = [("value_type", C.c_int), ("heavy_cols", C.c_int), ("heavy_nnz", C.c_int), ("light_nnz", C.c_int),
+                ("y_f32", C.c_int), ("device_bytes", C.c_size_t)]
+
+
 class PlanOptsC(C.Structure):
     _fields_ = [("with_reference_arrays", C.c_int), ("heavy_band", C.c_int), ("reserved", C.c_int * 6)]
 
@@ -77,6 +82,10 @@ SIGNATURES = [
     ("fl_plan_spmv", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p]),
     ("fl_plan_spmv_host", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
     ("fl_plan_destroy", C.c_int, [C.c_void_p]),
+    ("fl_plan_add_form", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int)]),
+    ("fl_plan_form_info", C.c_int, [C.c_void_p, C.c_int, C.POINTER(FormInfoC)]),
+    ("fl_plan_spmv_form", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
+    ("fl_plan_permute_x_k", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("fl_col_sort_noalloc", C.c_int, [C.c_int, C.c_int] + [C.c_void_p] * 11),
 ]
 

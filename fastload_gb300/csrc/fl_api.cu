@@ -18,13 +18,6 @@ void debug_fail_alloc_after(int n);
 
 using namespace fl;
 
-struct fl_plan {
-    Layout L;
-    bool has_ref = false;
-    std::unique_ptr<Bucket> bucket;    // bucketed form (heavy band), optional
-    DevBuf<double> stage_x, stage_y;  // device staging of fl_plan_spmv_host
-};
-
 namespace {
 
 constexpr long kMaxNnz = 0x7fffffffL - 65536;  // headroom for padding and item rounding
@@ -533,15 +526,61 @@ int fl_plan_spmv_host(fl_plan_t p, const double *h_xs, double *h_y, int variant,
     return FL_SUCCESS;
 }
 
+int fl_plan_add_form(fl_plan_t p, int value_type, int heavy_band, int y_f32, int *form_id) {
+    clear_error();
+    if (!p || !form_id) return fail(FL_ERR_ARG, "add_form: NULL argument");
+    std::unique_ptr<Form> F(new (std::nothrow) Form());
+    if (!F) return fail(FL_ERR_ALLOC, "add_form: host allocation failed");
+    FL_CUDA(cudaDeviceSynchronize());
+    FL_TRY(build_form(*F, p->L, value_type, heavy_band, y_f32 != 0, 0));
+    p->forms.push_back(std::move(F));
+    *form_id = (int)p->forms.size() - 1;
+    return FL_SUCCESS;
+}
+
+int fl_plan_form_info(fl_plan_t p, int form_id, fl_form_info *info) {
+    clear_error();
+    if (!p || !info || form_id < 0 || form_id >= (int)p->forms.size())
+        return fail(FL_ERR_ARG, "form_info: bad plan or form id");
+    const Form &F = *p->forms[form_id];
+    info->value_type = F.vtype;
+    info->heavy_cols = F.B.heavy.nnz > 0 ? F.B.heavy.nh : 0;
+    info->heavy_nnz = (int)F.B.heavy.nnz;
+    info->light_nnz = F.B.light.nnz;
+    info->y_f32 = F.yf32;
+    const size_t vs = F.vtype == FL_VALUES_F64 ? 8 : 4;
+    info->device_bytes = F.B.light.row.n * 4 + F.B.light.row.n * vs + F.B.heavy.padded * (vs + (F.wide ? 4 : 2)) +
+                         F.B.heavy.row.n * 8 + F.B.light.regions.item.n * sizeof(ItemDesc);
+    return FL_SUCCESS;
+}
+
+int fl_plan_spmv_form(fl_plan_t p, int form_id, int k, const void *d_xs, void *d_y, int accumulate, void *stream) {
+    if (!p || form_id < 0 || form_id >= (int)p->forms.size()) return fail(FL_ERR_ARG, "spmv_form: bad plan or form id");
+    if ((p->L.n && !d_xs) || (p->L.m && !d_y)) return fail(FL_ERR_ARG, "spmv_form: NULL argument");
+    return spmv_form(*p->forms[form_id], k, d_xs, d_y, accumulate, (cudaStream_t)stream);
+}
+
+int fl_plan_permute_x_k(fl_plan_t p, int k, int to_f32, const double *d_x, void *d_xs, void *stream) {
+    clear_error();
+    if (!p || (p->L.n && (!d_x || !d_xs))) return fail(FL_ERR_ARG, "permute_x_k: NULL argument");
+    if (k < 1) return fail(FL_ERR_ARG, "permute_x_k: k=%d", k);
+    return permute_x_k(p->L.perm.get(), p->L.n, k, d_x, d_xs, to_f32, (cudaStream_t)stream);
+}
+
 int fl_plan_check(fl_plan_t p) {
     clear_error();
     if (!p) return fail(FL_ERR_ARG, "plan_check: NULL plan");
     FL_CUDA(cudaDeviceSynchronize());
-    if (!p->bucket) return FL_SUCCESS;
-    int h = 0;
-    FL_CUDA(cudaMemcpy(&h, p->bucket->err.get(), sizeof(int), cudaMemcpyDeviceToHost));
-    FL_CUDA(cudaMemset(p->bucket->err.get(), 0, sizeof(int)));
-    if (h) return fail(FL_ERR_NOT_READY, "bucket kernel: staging of the heavy band's x did not complete (0x%x)", h);
+    std::vector<const Bucket *> all;
+    if (p->bucket) all.push_back(p->bucket.get());
+    for (auto &f : p->forms) all.push_back(&f->B);
+    for (const Bucket *b : all) {
+        if (!b->err.get()) continue;
+        int h = 0;
+        FL_CUDA(cudaMemcpy(&h, b->err.get(), sizeof(int), cudaMemcpyDeviceToHost));
+        FL_CUDA(cudaMemset(b->err.get(), 0, sizeof(int)));
+        if (h) return fail(FL_ERR_NOT_READY, "staging of the heavy band's x did not complete (0x%x)", h);
+    }
     return FL_SUCCESS;
 }
 

@@ -68,7 +68,7 @@ __global__ void k_slice_width(const unsigned *rows, const int *rlen, int nslices
 // slice_ptr[s] + 32 j + l (zero padding past the row's length).
 __global__ void k_slice_fill(const unsigned *rows, const int *rlen, const int *rp, const int *hc,
                              const double *hv, int nrows, int nslices, const int *slice_ptr, double *val,
-                             uint16_t *col, int *srow, int *slen) {
+                             uint16_t *col, int *col32, int *srow, int *slen) {
     const int lane = threadIdx.x & 31;
     long gw = (blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5, nw = ((long)gridDim.x * blockDim.x) >> 5;
     for (long s = gw; s < nslices; s += nw) {
@@ -82,7 +82,8 @@ __global__ void k_slice_fill(const unsigned *rows, const int *rlen, const int *r
         for (int j = 0; j < w; j++) {
             const long dst = base + 32L * j + lane;
             val[dst] = j < len ? hv[src + j] : 0.0;
-            col[dst] = j < len ? (uint16_t)hc[src + j] : (uint16_t)0;
+            if (col) col[dst] = j < len ? (uint16_t)hc[src + j] : (uint16_t)0;
+            else col32[dst] = j < len ? hc[src + j] : 0;
         }
     }
 }
@@ -117,8 +118,9 @@ int bucket_auto_band(const int *sortnnz, int n, int nnz, cudaStream_t s) {
 }
 
 int build_bucket(Bucket &B, int m, int n, int nnz, const int *sortnnz, const int *srow_tmp,
-                 const double *sval_tmp, int nh, cudaStream_t s) {
-    nh = std::max(0, std::min(nh, std::min(n, BK_MAX_BAND))) & ~1;
+                 const double *sval_tmp, int nh, cudaStream_t s, bool wide) {
+    nh = std::max(0, std::min(nh, wide ? n : std::min(n, BK_MAX_BAND)));
+    if (!wide || nh < n) nh &= ~1;
     const int H0 = n - nh;
     DevBuf<int> scolptr;
     FL_TRY(scolptr.alloc((size_t)n + 1, s));
@@ -176,12 +178,14 @@ int build_bucket(Bucket &B, int m, int n, int nnz, const int *sortnnz, const int
     FL_TRY(read_ints(s, H.slice_ptr.get() + H.nslices, &total, 1));
     H.padded = total;
     FL_TRY(H.val.alloc(std::max(total, 1), s));
-    FL_TRY(H.col.alloc(std::max(total, 1), s));
+    const bool narrow = nh <= 65535;
+    if (narrow) FL_TRY(H.col.alloc(std::max(total, 1), s));
+    else FL_TRY(H.col32.alloc(std::max(total, 1), s));
     FL_TRY(H.row.alloc(32L * H.nslices, s));
     FL_TRY(H.len.alloc(32L * H.nslices, s));
     k_slice_fill<<<grid_cap(32L * H.nslices, 256, 16), 256, 0, s>>>(
         rows.get(), rlen.get(), rp.get(), hc.get(), hv.get(), H.nrows, H.nslices, H.slice_ptr.get(), H.val.get(),
-        H.col.get(), H.row.get(), H.len.get());
+        narrow ? H.col.get() : nullptr, narrow ? nullptr : H.col32.get(), H.row.get(), H.len.get());
     FL_CUDA(cudaGetLastError());
     FL_CUDA(cudaStreamSynchronize(s));
     return FL_SUCCESS;

@@ -134,7 +134,8 @@ struct HeavyBand {
     long nnz = 0;               // band nonzeros (no padding)
     long padded = 0;            // slice entries including padding
     DevBuf<double> val;
-    DevBuf<uint16_t> col;
+    DevBuf<uint16_t> col;       // local columns when nh <= 65535
+    DevBuf<int> col32;          // local columns of wider bands
     DevBuf<int> slice_ptr;      // nslices+1
     DevBuf<int> row;            // 32*nslices, -1 for an empty lane
     DevBuf<int> len;            // 32*nslices
@@ -148,6 +149,35 @@ struct Bucket {
     DevBuf<int> err;            // device status word of the bucket kernel
     DevBuf<int> next;           // work counter of the bucket kernel (zeroed per launch)
 };
+
+// A storage / right-hand-side form of a plan: its own bucketed split (light
+// FastLoad stream + heavy band in row slices) with values in the form's
+// storage type.  FP64 forms use the bucket's FP64 arrays directly.
+struct Form {
+    int vtype = 0;             // FL_VALUES_F64 / F32 / BF16X2
+    int yf32 = 0;              // y accumulated in FP32 instead of FP64
+    int band = 0;              // heavy band requested (FL_BAND_*)
+    bool wide = false;         // band columns stored as 32-bit indices
+    Bucket B;
+    DevBuf<unsigned char> lval, hval;  // converted values (F32 / BF16X2 forms)
+};
+
+// Step table as raw pointers for kernels.
+struct StepView {
+    const int *col, *base, *tall, *tile_off, *nnz_off;
+    int steps;
+};
+
+// Largest i in [0, cnt) with a[i] <= v (a non-decreasing, a[0] <= v).
+__device__ __forceinline__ int upper_index(const int *__restrict__ a, int cnt, int v) {
+    int lo = 0, hi = cnt - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (__ldg(a + mid) <= v) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
 
 constexpr int FL_PAD = 512;     // stream padding granularity (entries)
 constexpr int FL_ITEM = 2048;   // nonzeros per work item of the stream kernel
@@ -199,8 +229,10 @@ int spmv_stream_f64(const Layout &L, const double *xs, double *y, int variant,
                     cudaStream_t s);
 int spmv_tile_f64(const Layout &L, const double *xs, double *y, cudaStream_t s);
 // Bucketed form: build from the column-sorted CSC (device) and run.
+// wide: allow a band of up to all n columns (x then read from global memory
+// by the form kernels); otherwise the band is capped at bucket_max_band().
 int build_bucket(Bucket &B, int m, int n, int nnz, const int *sortnnz, const int *srow_tmp,
-                 const double *sval_tmp, int nh, cudaStream_t s);
+                 const double *sval_tmp, int nh, cudaStream_t s, bool wide = false);
 int spmv_bucket_f64(const Bucket &B, const double *xs, double *y, cudaStream_t s);
 // Largest heavy band the bucket kernel can stage in shared memory.
 int bucket_max_band();
@@ -211,4 +243,20 @@ int bucket_auto_band(const int *sortnnz, int n, int nnz, cudaStream_t s);
 
 int num_sms();
 
+// Forms (fl_form.cu): build from a plan's FP64 layout, run.
+int build_form(Form &F, const Layout &L, int vtype, int band, int yf32, cudaStream_t s);
+int spmv_form(Form &F, int k, const void *xs, void *y, int accumulate, cudaStream_t s);
+int permute_x_k(const int *perm, int n, int k, const double *x, void *xs, int to_f32, cudaStream_t s);
+
 }  // namespace fl
+
+// The plan object behind fl_plan_t.
+#include <memory>
+#include <vector>
+struct fl_plan {
+    fl::Layout L;
+    bool has_ref = false;
+    std::unique_ptr<fl::Bucket> bucket;           // bucketed FP64 form (heavy band), optional
+    std::vector<std::unique_ptr<fl::Form>> forms; // storage / rhs forms
+    fl::DevBuf<double> stage_x, stage_y;          // device staging of fl_plan_spmv_host
+};

@@ -300,17 +300,6 @@ __global__ void k_iota(unsigned *a, long n) {
         a[i] = (unsigned)i;
 }
 
-// Largest i in [0, cnt) with a[i] <= v (a non-decreasing, a[0] <= v).
-__device__ __forceinline__ int upper_index(const int *__restrict__ a, int cnt, int v) {
-    int lo = 0, hi = cnt - 1;
-    while (lo < hi) {
-        int mid = (lo + hi + 1) >> 1;
-        if (__ldg(a + mid) <= v) lo = mid;
-        else hi = mid - 1;
-    }
-    return lo;
-}
-
 // Reads back a few device ints with one synchronisation.
 static int read_back(cudaStream_t s, const int *dev, int *host, int count) {
     FL_CUDA(cudaMemcpyAsync(host, dev, count * sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -487,11 +476,6 @@ __global__ void k_step_fill(const int *sortnnz, const int *flag, const int *step
     }
     if (local) atomicAdd(tiles64, local);
 }
-
-struct StepView {
-    const int *col, *base, *tall, *tile_off, *nnz_off;
-    int steps;
-};
 
 // One warp per tile.  Tile t of step s is (chunk c, level l) with
 // q = t - tile_off[s] = c * tall + l; its payload starts at

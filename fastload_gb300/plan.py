@@ -10,7 +10,7 @@ import ctypes as C
 
 import numpy as np
 
-from ._lib import PlanInfoC, PlanOptsC, SlideMatrixC, check, load
+from ._lib import FormInfoC, PlanInfoC, PlanOptsC, SlideMatrixC, check, load
 from .host import SlideMatrix
 
 KERNEL_AUTO = 0
@@ -20,6 +20,12 @@ KERNEL_STREAM2 = 3
 KERNEL_BUCKET = 4
 INPUT_CSR = 0
 INPUT_CSC = 1
+VALUES_F64 = 0
+VALUES_F32 = 1
+VALUES_BF16X2 = 2
+BAND_AUTO = 0
+BAND_NONE = -1
+BAND_ALL = -2
 
 
 def _torch():
@@ -122,6 +128,39 @@ class Plan:
             y = np.empty(self.m, np.float64)
         check(load().fl_plan_spmv_host(self._h, C.c_void_p(xs.ctypes.data), C.c_void_p(y.ctypes.data),
                                        int(kernel), _stream_handle(stream)))
+        return y
+
+    # -- forms ---------------------------------------------------------------
+    def add_form(self, value_type: int = VALUES_F32, heavy_band: int = BAND_AUTO, y_f32: bool = False) -> int:
+        """Adds a storage form (FP64 / FP32 / BF16 hi+lo values) with the given
+        heavy band; returns its id for spmv_form."""
+        fid = C.c_int(-1)
+        check(load().fl_plan_add_form(self._h, int(value_type), int(heavy_band), int(y_f32), C.byref(fid)))
+        return fid.value
+
+    def form_info(self, form_id: int) -> dict:
+        i = FormInfoC()
+        check(load().fl_plan_form_info(self._h, int(form_id), C.byref(i)))
+        return {k: getattr(i, k) for k, _ in FormInfoC._fields_}
+
+    def permute_x_k(self, x, k: int = 1, to_f32: bool = False, stream=None):
+        """x (n*k, row-interleaved, float64) -> sorted column order, float32
+        when to_f32."""
+        torch = _torch()
+        x = _dev(x, torch.float64).reshape(-1)
+        xs = torch.empty(self.n * k, dtype=torch.float32 if to_f32 else torch.float64, device="cuda")
+        check(load().fl_plan_permute_x_k(self._h, int(k), int(to_f32), C.c_void_p(x.data_ptr()),
+                                         C.c_void_p(xs.data_ptr()), _stream_handle(stream)))
+        return xs
+
+    def spmv_form(self, form_id: int, xs, y=None, k: int = 1, accumulate: bool = False, y_f32: bool = False,
+                  stream=None):
+        torch = _torch()
+        if y is None:
+            y = torch.empty(self.m * k, dtype=torch.float32 if y_f32 else torch.float64, device="cuda")
+            accumulate = False
+        check(load().fl_plan_spmv_form(self._h, int(form_id), int(k), C.c_void_p(xs.data_ptr()),
+                                       C.c_void_p(y.data_ptr()), int(accumulate), _stream_handle(stream)))
         return y
 
     def check(self) -> None:

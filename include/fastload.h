@@ -197,6 +197,39 @@ int fl_plan_destroy(fl_plan_t plan);
  * bounded wait expired); synchronises the device. */
 int fl_plan_check(fl_plan_t plan);
 
+/* ---- storage / right-hand-side forms ---------------------------------- */
+
+/* Value storage of a form. */
+#define FL_VALUES_F64 0    /* FP64 values, FP64 products (x and y FP64) */
+#define FL_VALUES_F32 1    /* FP32 values, FP32 x, FP32 products */
+#define FL_VALUES_BF16X2 2 /* BF16 hi+lo split (v ~ hi + lo), FP32 x, FP32 products */
+/* Heavy band of a form (columns handled in 32-row slices, one lane per row). */
+#define FL_BAND_AUTO 0     /* the plan's automatic choice */
+#define FL_BAND_NONE (-1)  /* pure FastLoad tile stream (one atomic per run) */
+#define FL_BAND_ALL (-2)   /* every column: rows owned by one lane, no atomics */
+
+typedef struct fl_form_info {
+    int value_type, heavy_cols, heavy_nnz, light_nnz, y_f32;
+    size_t device_bytes;
+} fl_form_info;
+
+/* Adds a form to the plan: values stored as value_type, the given heavy band
+ * (FL_BAND_* or a column count), y accumulated in FP32 when y_f32 != 0 (FP32
+ * values only) else FP64.  *form_id receives the form's index.  Products and
+ * per-row sums are FP32 for FP32/BF16 forms and FP64 for FP64 forms. */
+int fl_plan_add_form(fl_plan_t plan, int value_type, int heavy_band, int y_f32,
+                     int *form_id);
+int fl_plan_form_info(fl_plan_t plan, int form_id, fl_form_info *info);
+/* y = A xs (or += when accumulate) for k right-hand sides (k = 1 or 8):
+ * xs[(sorted column)*k + r] (double for FP64 forms, float otherwise; see
+ * fl_plan_permute_x_k), y[row*k + r] (double, or float for y_f32 forms).
+ * For k > 1 both must be 16-byte aligned.  Asynchronous on `stream`. */
+int fl_plan_spmv_form(fl_plan_t plan, int form_id, int k, const void *d_xs,
+                      void *d_y, int accumulate, void *stream);
+/* xs[i*k + r] = x[perm[i]*k + r], converted to float when to_f32 != 0. */
+int fl_plan_permute_x_k(fl_plan_t plan, int k, int to_f32, const double *d_x,
+                        void *d_xs, void *stream);
+
 /* ---- allocation-free column sort -------------------------------------- */
 
 /* Largest column count fl_col_sort_noalloc accepts (its scratch array holds
