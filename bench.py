@@ -197,6 +197,116 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def _time_ms(fn, reps, flush=None):
+    """Mean device time of fn() over reps, with an optional L2 flush before
+    each timed call (events bracket fn only)."""
+    import torch
+
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for _ in range(3):
+        fn()
+    ts = []
+    for _ in range(reps):
+        if flush is not None:
+            flush.zero_()
+        a.record()
+        fn()
+        b.record()
+        b.synchronize()
+        ts.append(a.elapsed_time(b))
+    return float(np.mean(ts))
+
+
+def measure_forms(fl, peak, reps=30):
+    """Storage / multi-RHS forms against the plain FP64 kernel on the same
+    inputs: the 128^3 7-point Laplacian (k = 1 and 8) and the Zipf matrix.
+    GB/s by each form's algorithmic bytes, L2 flushed before every timed run."""
+    import torch
+
+    import oracle
+    from fastload_gb300 import gen
+
+    flush = torch.empty(64 << 20, dtype=torch.float32, device="cuda")  # 256 MB > 129 MB L2
+    out = {}
+
+    def entry(c, t_ms, k, s_val, s_x, y, yref, plain_gflops=None):
+        B = algorithmic_bytes(c.m, c.n, c.nnz, s_val=s_val, s_idx=4, s_x=s_x, s_y=8, k=k)
+        gflops = 2.0 * c.nnz * k / (t_ms * 1e-3) / 1e9
+        nw, mx = oracle.rel_errors(np.asarray(y).reshape(-1), np.asarray(yref).reshape(-1))
+        d = {"ms": t_ms, "gbs": B / (t_ms * 1e-3) / 1e9, "pct_of_peak": 100.0 * B / (t_ms * 1e-3) / 1e9 / peak,
+             "gflops": gflops, "rel_err_normwise": nw, "rel_err_max": mx}
+        if plain_gflops:
+            d["gflops_vs_plain_fp64"] = gflops / plain_gflops
+        return d
+
+    forms = [("f64", fl.VALUES_F64, 8), ("f32", fl.VALUES_F32, 4), ("bf16x2", fl.VALUES_BF16X2, 4)]
+    cases = [("lap128", gen.laplacian7(128, seed=4), [("band_none", fl.BAND_NONE), ("band_all", fl.BAND_ALL)]),
+             ("zipf_n1048576", make_workload(N_COLS), [("band_auto", fl.BAND_AUTO), ("band_none", fl.BAND_NONE)])]
+    for cname, c, bands in cases:
+        rng = np.random.default_rng(11)
+        x8 = rng.uniform(-1, 1, c.n * 8)
+        ref = {1: oracle.csc_spmv_dd(c.m, c.n, c.colptr, c.rowidx, c.val, c.x)}
+        if not cname.startswith("zipf"):
+            ref[8] = oracle.csc_spmv_dd(c.m, c.n, c.colptr, c.rowidx, c.val, x8, k=8)
+        xin = {1: c.x, 8: x8}
+        with fl.Plan.from_csc(c.m, c.n, c.colptr, c.rowidx, c.val) as p:
+            xs = p.permute_x(torch.from_numpy(c.x).cuda())
+            y = torch.empty(c.m, dtype=torch.float64, device="cuda")
+            t = _time_ms(lambda: p.spmv(xs, y, kernel=fl.KERNEL_STREAM2), reps, flush)
+            plain = entry(c, t, 1, 8, 8, y.cpu().numpy(), ref[1])
+            out[f"{cname}_plain_fp64_stream_k1"] = plain
+            for bname, band in bands:
+                for fname, vt, sv in forms:
+                    fid = p.add_form(vt, band)
+                    for k in (1, 8):
+                        if cname.startswith("zipf") and k == 8:
+                            continue
+                        xk = p.permute_x_k(torch.from_numpy(xin[k]).cuda(), k=k, to_f32=vt != fl.VALUES_F64)
+                        yk = torch.empty(c.m * k, dtype=torch.float64, device="cuda")
+                        t = _time_ms(lambda: p.spmv_form(fid, xk, yk, k=k), reps, flush)
+                        sx = 8 if vt == fl.VALUES_F64 else 4
+                        out[f"{cname}_{fname}_{bname}_k{k}"] = entry(
+                            c, t, k, sv, sx, yk.cpu().numpy(), ref[k], plain["gflops"])
+            p.check()
+        del c
+    return out
+
+
+def run_profile(spec):
+    """--profile case:values:band:k -- builds one case and runs one kernel a
+    few times (for ncu captures).  case lap128 | zipf | zipf<n>; values
+    f64 | f32 | bf16x2 | plain (the plain FP64 stream kernel) | bucket (the
+    FP64 bucketed kernel); band auto | none | all | <columns>; k 1 | 8."""
+    import torch
+
+    import fastload_gb300 as fl
+    from fastload_gb300 import gen
+
+    case, vals, band, k = spec.split(":")
+    k = int(k)
+    if case == "lap128":
+        c = gen.laplacian7(128, seed=4)
+    else:
+        c = make_workload(int(case[4:]) if case != "zipf" else N_COLS)
+    with fl.Plan.from_csc(c.m, c.n, c.colptr, c.rowidx, c.val) as p:
+        x = torch.from_numpy(np.random.default_rng(11).uniform(-1, 1, c.n * k)).cuda()
+        if vals in ("plain", "bucket"):
+            xs = p.permute_x(x[: c.n])
+            y = torch.empty(c.m, dtype=torch.float64, device="cuda")
+            kern = fl.KERNEL_STREAM2 if vals == "plain" else fl.KERNEL_BUCKET
+            fn = lambda: p.spmv(xs, y, kernel=kern)  # noqa: E731
+        else:
+            vt = {"f64": fl.VALUES_F64, "f32": fl.VALUES_F32, "bf16x2": fl.VALUES_BF16X2}[vals]
+            bd = {"auto": fl.BAND_AUTO, "none": fl.BAND_NONE, "all": fl.BAND_ALL}.get(band)
+            fid = p.add_form(vt, bd if bd is not None else int(band))
+            xs = p.permute_x_k(x, k=k, to_f32=vt != fl.VALUES_F64)
+            y = torch.empty(c.m * k, dtype=torch.float64, device="cuda")
+            fn = lambda: p.spmv_form(fid, xs, y, k=k)  # noqa: E731
+        ms = _time_ms(fn, 5)
+        p.check()
+    print(json.dumps({"profile": spec, "nnz": c.nnz, "ms": ms}), flush=True)
+
+
 def run_gpu(args, rank, world):
     import torch
 
@@ -297,6 +407,8 @@ def run_gpu(args, rank, world):
     e2e_s = (time.perf_counter() - t0) / ke
     e2e_rel = oracle.rel_errors(hy, ydd)
 
+    peak, peak_kind = measured_peaks()
+    forms = measure_forms(fl, peak) if (rank == 0 and not args.quick and not args.no_forms) else None
     if rank != 0:
         if dist:
             dist.destroy_process_group()
@@ -321,6 +433,7 @@ def run_gpu(args, rank, world):
         "kernel_variants_gbs": variants,
         "speedup_vs_plain_fp64_stream": (variants["stream2"] and achieved / variants["stream2"]) if variants else None,
         "preprocess_s": prep_s,
+        "forms": forms,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_kind": f"{peak_kind} hbm_gbs",
                      "kernel": kname, "bytes_per_launch": B, "kernel_ms": kern_ms},
@@ -344,12 +457,16 @@ def main():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="fastload", choices=["fastload", "reference"])
     ap.add_argument("--n", type=int, default=N_COLS, help="columns of the Zipf matrix (default 1,048,576)")
+    ap.add_argument("--profile", default=None, help="case:values:band:k -- run one kernel for a profiler")
+    ap.add_argument("--no-forms", action="store_true", help="skip the storage / multi-RHS form measurements")
     ap.add_argument("--quick", action="store_true", help="skip kernel variants, shorten e2e and CPU legs "
                                                          "(for profiling runs)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", args.gpus if args.gpus == 1 else 1))
-    if args.impl == "reference":
+    if args.profile:
+        run_profile(args.profile)
+    elif args.impl == "reference":
         run_reference(args, rank, world)
     else:
         run_gpu(args, rank, world)

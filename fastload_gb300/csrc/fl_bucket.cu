@@ -17,19 +17,16 @@
 // 500 G/s) are the scarce resources of a CSC SpMV; the heavy band turns one
 // atomic per nonzero into one per row and keeps exactly one FP64 operation
 // per nonzero.  One persistent launch runs both parts.
-#include "fl_stream.cuh"
+#include "fl_forms.cuh"
 
 #include <algorithm>
 #include <vector>
 
 namespace fl {
 
-constexpr int BK_THREADS = 1024;
 constexpr int BK_MAX_BAND = 24576;            // 192 KB of FP64 x in shared memory
 constexpr int BK_AUTO_BAND = 16384;           // default band width cap
 constexpr int BK_AUTO_MIN_DEGREE = 32;        // densest columns worth a row slice
-constexpr long BK_WAIT_LIMIT = 1L << 20;      // bounded mbarrier polling
-constexpr int HV_UNROLL = 4;                  // heavy-slice loads in flight per lane
 
 int bucket_max_band() { return BK_MAX_BAND; }
 
@@ -183,6 +180,28 @@ int build_bucket(Bucket &B, int m, int n, int nnz, const int *sortnnz, const int
     else FL_TRY(H.col32.alloc(std::max(total, 1), s));
     FL_TRY(H.row.alloc(32L * H.nslices, s));
     FL_TRY(H.len.alloc(32L * H.nslices, s));
+    // work units: runs of consecutive slices, sized so the units number
+    // about four per resident warp (never less than one slice) -- enough
+    // units to balance, few enough that the work counter stays cold
+    {
+        std::vector<int> sp(H.nslices + 1);
+        FL_TRY(read_ints(s, H.slice_ptr.get(), sp.data(), H.nslices + 1));
+        std::vector<int> ub(1, 0);
+        const long target_units = 4L * num_sms() * 32;
+        const long per_unit = std::max<long>(1, (long)sp[H.nslices] / target_units);
+        long acc = 0;
+        for (int q = 0; q < H.nslices; q++) {
+            acc += sp[q + 1] - sp[q];
+            if (acc >= per_unit || q == H.nslices - 1) {
+                ub.push_back(q + 1);
+                acc = 0;
+            }
+        }
+        H.nunits = (int)ub.size() - 1;
+        FL_TRY(H.unit_slice.alloc(ub.size(), s));
+        FL_CUDA(cudaMemcpyAsync(H.unit_slice.get(), ub.data(), ub.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+        FL_CUDA(cudaStreamSynchronize(s));
+    }
     k_slice_fill<<<grid_cap(32L * H.nslices, 256, 16), 256, 0, s>>>(
         rows.get(), rlen.get(), rp.get(), hc.get(), hv.get(), H.nrows, H.nslices, H.slice_ptr.get(), H.val.get(),
         narrow ? H.col.get() : nullptr, narrow ? nullptr : H.col32.get(), H.row.get(), H.len.get());
@@ -192,152 +211,15 @@ int build_bucket(Bucket &B, int m, int n, int nnz, const int *sortnnz, const int
 }
 
 // ------------------------------------------------------------ kernel ----
-struct BucketArgs {
-    // light part
-    const ItemDesc *items;
-    const RegionDesc *regions;
-    const int *row;
-    const double *val;
-    int nitems;
-    // heavy band
-    int H0, nh, nslices, bulk;
-    const int *slice_ptr, *hrow, *hlen;
-    const double *hval;
-    const uint16_t *hcol;
-    const double *xs;
-    double *y;
-    int *err;
-    int *next;  // work counter: units [0, nitems) are light items, then heavy slices
-};
-
-__device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t phase) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(bar), "r"(phase)
-        : "memory");
-    return ok != 0;
-}
-
-__device__ __forceinline__ double ld_stream_f64(const double *p) {
-    double r;
-    asm("ld.global.nc.L1::no_allocate.f64 %0, [%1];" : "=d"(r) : "l"(p));
-    return r;
-}
-__device__ __forceinline__ unsigned short ld_stream_u16(const uint16_t *p) {
-    unsigned short r;
-    asm("ld.global.nc.L1::no_allocate.u16 %0, [%1];" : "=h"(r) : "l"(p));
-    return r;
-}
-
-template <int U>
-__global__ void __launch_bounds__(BK_THREADS, 1) k_spmv_bucket_f64(const BucketArgs a) {
-    extern __shared__ __align__(128) double xh[];
-    __shared__ __align__(8) unsigned long long mbar;
-    const int tid = threadIdx.x, lane = tid & 31;
-    const int gw = (blockIdx.x * blockDim.x + tid) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
-    const uint32_t bar = smem_addr(&mbar);
-    if (a.nh > 0) {
-        if (a.bulk) {
-            if (tid == 0) {
-                asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
-                asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-            }
-            __syncthreads();
-            if (tid == 0) {
-                const uint32_t bytes = (uint32_t)a.nh * 8u;
-                asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
-                             : "memory");
-                const char *src = (const char *)(a.xs + a.H0);
-                const uint32_t dst = smem_addr(xh);
-                for (uint32_t off = 0; off < bytes; off += 32768u) {
-                    const uint32_t sz = min(32768u, bytes - off);
-                    asm volatile(
-                        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
-                            "r"(dst + off),
-                        "l"(src + off), "r"(sz), "r"(bar)
-                        : "memory");
-                }
-            }
-        } else {
-            for (int i = tid; i < a.nh; i += blockDim.x) xh[i] = __ldg(a.xs + a.H0 + i);
-            __syncthreads();
-        }
-    }
-    // Work units are handed out by a counter: light items first (the band's
-    // x arrives meanwhile), then heavy slices widest first, so every warp
-    // keeps busy until the last unit.
-    const int total = a.nitems + (a.nh > 0 ? a.nslices : 0);
-    bool staged = !(a.nh > 0 && a.bulk);
-    for (;;) {
-        int u = 0;
-        if (lane == 0) u = atomicAdd(a.next, 1);
-        u = __shfl_sync(FULLM, u, 0);
-        if (u >= total) break;
-        if (u < a.nitems) {
-            stream_item_f64<U>(a.items[u], a.regions, a.row, a.val, a.xs, a.y, lane);
-            continue;
-        }
-        if (!staged) {
-            bool ok = false;
-            for (long i = 0; i < BK_WAIT_LIMIT && !ok; i++) ok = mbar_try_wait(bar, 0);
-            if (!ok) {
-                if (lane == 0) atomicOr(a.err, 1);
-                break;
-            }
-            staged = true;
-        }
-        // heavy slice: one lane per row
-        const int sl = u - a.nitems;
-        const int base = __ldg(a.slice_ptr + sl);
-        const int w = (__ldg(a.slice_ptr + sl + 1) - base) >> 5;
-        const int r = __ldg(a.hrow + 32 * sl + lane), len = __ldg(a.hlen + 32 * sl + lane);
-        const double *vp = a.hval + base + lane;
-        const uint16_t *cp = a.hcol + base + lane;
-        double acc = 0.0;
-        int j = 0;
-        for (; j + HV_UNROLL <= w; j += HV_UNROLL) {
-            double v[HV_UNROLL];
-            unsigned short c[HV_UNROLL];
-#pragma unroll
-            for (int k = 0; k < HV_UNROLL; k++) {
-                if (j + k < len) {
-                    v[k] = ld_stream_f64(vp + 32 * (j + k));
-                    c[k] = ld_stream_u16(cp + 32 * (j + k));
-                }
-            }
-#pragma unroll
-            for (int k = 0; k < HV_UNROLL; k++)
-                if (j + k < len) acc = fma(v[k], xh[c[k]], acc);
-        }
-        for (; j < w; j++)
-            if (j < len) acc = fma(ld_stream_f64(vp + 32 * j), xh[ld_stream_u16(cp + 32 * j)], acc);
-        if (len > 0) atomicAdd(a.y + r, acc);
-    }
-    // a block must not exit while its bulk copy may still write its shared
-    // memory: wait (bounded) when no warp of this block waited yet
-    if (a.nh > 0 && a.bulk && !staged) {
-        bool ok = false;
-        for (long i = 0; i < BK_WAIT_LIMIT && !ok; i++) ok = mbar_try_wait(bar, 0);
-        if (!ok && lane == 0) atomicOr(a.err, 2);
-    }
-}
+// The FP64 bucketed SpMV is the FP64, one right-hand-side instance of the
+// generic form kernel (fl_forms.cuh): light items through the FastLoad stream,
+// heavy units with x staged in shared memory by a TMA bulk copy.
+int run_form_f64(const FormArgs<double, double> &a, int k, bool wide, cudaStream_t s);
 
 int spmv_bucket_f64(const Bucket &B, const double *xs, double *y, cudaStream_t s) {
     const HeavyBand &H = B.heavy;
     const Regions &R = B.light.regions;
-    static bool attr_set = false;
-    if (!attr_set) {
-        FL_CUDA(cudaFuncSetAttribute(k_spmv_bucket_f64<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     BK_MAX_BAND * (int)sizeof(double)));
-        attr_set = true;
-    }
-    BucketArgs a;
+    FormArgs<double, double> a;
     a.items = R.item.get();
     a.regions = R.region.get();
     a.row = B.light.row.get();
@@ -345,28 +227,25 @@ int spmv_bucket_f64(const Bucket &B, const double *xs, double *y, cudaStream_t s
     a.nitems = R.nitems;
     a.H0 = H.H0;
     a.nh = H.nnz > 0 ? H.nh : 0;
-    a.nslices = H.nslices;
+    a.nslices = H.nnz > 0 ? H.nslices : 0;
+    a.nunits = H.nnz > 0 ? H.nunits : 0;
+    a.unit_slice = H.unit_slice.get();
     a.slice_ptr = H.slice_ptr.get();
     a.hrow = H.row.get();
     a.hlen = H.len.get();
     a.hval = H.val.get();
-    a.hcol = H.col.get();
+    a.hcol16 = H.col.get();
+    a.hcol32 = H.col32.get();
     a.xs = xs;
     a.y = y;
     a.err = B.err.get();
     a.next = B.next.get();
+    a.heavy_mode = 0;
     const size_t bytes = (size_t)a.nh * sizeof(double);
     a.bulk = a.nh > 0 && ((uintptr_t)(xs + H.H0) % 16 == 0) && bytes % 16 == 0;
-    if (a.nitems == 0 && a.nslices == 0) return FL_SUCCESS;
+    if (a.nitems == 0 && a.nunits == 0) return FL_SUCCESS;
     FL_CUDA(cudaMemsetAsync(a.next, 0, sizeof(int), s));
-    int per_sm = 0;
-    FL_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_spmv_bucket_f64<2>, BK_THREADS, bytes));
-    if (per_sm <= 0) per_sm = 1;
-    const long warps_needed = (long)a.nitems + a.nslices;
-    const long grid = std::max<long>(1, std::min<long>((long)num_sms() * per_sm, (warps_needed + 31) / 32));
-    k_spmv_bucket_f64<2><<<(int)grid, BK_THREADS, bytes, s>>>(a);
-    FL_CUDA(cudaGetLastError());
-    return FL_SUCCESS;
+    return run_form_f64(a, 1, H.nh > 65535, s);
 }
 
 }  // namespace fl

@@ -137,6 +137,8 @@ static FormArgs<V, Y> form_args(Form &F, const V *lval, const V *hval, const voi
     a.H0 = H.H0;
     a.nh = H.nnz > 0 ? H.nh : 0;
     a.nslices = H.nnz > 0 ? H.nslices : 0;
+    a.nunits = H.nnz > 0 ? H.nunits : 0;
+    a.unit_slice = H.unit_slice.get();
     a.slice_ptr = H.slice_ptr.get();
     a.hrow = H.row.get();
     a.hlen = H.len.get();
@@ -147,7 +149,7 @@ static FormArgs<V, Y> form_args(Form &F, const V *lval, const V *hval, const voi
     a.y = (Y *)y;
     a.err = B.err.get();
     a.next = B.next.get();
-    a.atomic_heavy = a.nitems > 0 ? 1 : 0;
+    a.heavy_mode = 0;
     a.bulk = 0;
     return a;
 }
@@ -160,8 +162,13 @@ int spmv_form(Form &F, int k, const void *xs, void *y, int accumulate, cudaStrea
     const size_t xsz = F.vtype == FL_VALUES_F64 ? sizeof(double) : sizeof(float);
     if (k > 1 && (((uintptr_t)xs % 16) || ((uintptr_t)y % 16)))
         return fail(FL_ERR_ARG, "spmv_form: x and y must be 16-byte aligned for k > 1");
-    if (!accumulate && m) FL_CUDA(cudaMemsetAsync(y, 0, (size_t)m * k * ysz, s));
-    if (B.light.regions.nitems == 0 && (B.heavy.nnz == 0)) return FL_SUCCESS;
+    // the heavy band owns whole rows when there is no light part: then y is
+    // updated without atomics, and written without zeroing first when every
+    // row has band nonzeros
+    const bool light = B.light.regions.nitems > 0;
+    const int mode = light ? 0 : (!accumulate && B.heavy.nrows == m ? 2 : 1);
+    if (!accumulate && m && mode != 2) FL_CUDA(cudaMemsetAsync(y, 0, (size_t)m * k * ysz, s));
+    if (!light && B.heavy.nnz == 0) return FL_SUCCESS;
     FL_CUDA(cudaMemsetAsync(B.next.get(), 0, sizeof(int), s));
     const HeavyBand &H = B.heavy;
     const size_t band_bytes = (size_t)H.nh * k * xsz;
@@ -170,20 +177,24 @@ int spmv_form(Form &F, int k, const void *xs, void *y, int accumulate, cudaStrea
     if (F.vtype == FL_VALUES_F64) {
         auto a = form_args<double, double>(F, B.light.val.get(), B.heavy.val.get(), xs, y);
         a.bulk = bulk;
+        a.heavy_mode = mode;
         return run_form_f64(a, k, F.wide, s);
     }
     if (F.vtype == FL_VALUES_F32) {
         if (F.yf32) {
             auto a = form_args<float, float>(F, (const float *)F.lval.get(), (const float *)F.hval.get(), xs, y);
             a.bulk = bulk;
+            a.heavy_mode = mode;
             return run_form_f32_y32(a, k, F.wide, s);
         }
         auto a = form_args<float, double>(F, (const float *)F.lval.get(), (const float *)F.hval.get(), xs, y);
         a.bulk = bulk;
+        a.heavy_mode = mode;
         return run_form_f32(a, k, F.wide, s);
     }
     auto a = form_args<bf16x2_t, double>(F, (const bf16x2_t *)F.lval.get(), (const bf16x2_t *)F.hval.get(), xs, y);
     a.bulk = bulk;
+    a.heavy_mode = mode;
     return run_form_bf16(a, k, F.wide, s);
 }
 

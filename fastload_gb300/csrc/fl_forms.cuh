@@ -23,75 +23,9 @@
 
 namespace fl {
 
-struct bf16x2_t {
-    uint32_t u;
-};
-
 constexpr int FM_THREADS = 1024;
 constexpr long FM_WAIT_LIMIT = 1L << 20;
 constexpr int FM_SMEM_MAX = 196608;  // dynamic shared memory budget of the form kernels
-
-__device__ __forceinline__ float bf16x2_decode(uint32_t u) {
-    return __uint_as_float(u << 16) + __uint_as_float(u & 0xffff0000u);
-}
-
-template <typename V>
-struct VT;
-
-template <>
-struct VT<double> {
-    using X = double;
-    using A = double;
-    static __device__ __forceinline__ void load4(const double *p, A v[4]) {
-        double2 a, b;
-        asm("ld.global.nc.L1::no_allocate.v2.f64 {%0,%1}, [%2];" : "=d"(a.x), "=d"(a.y) : "l"(p));
-        asm("ld.global.nc.L1::no_allocate.v2.f64 {%0,%1}, [%2];" : "=d"(b.x), "=d"(b.y) : "l"(p + 2));
-        v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
-    }
-    static __device__ __forceinline__ A stream1(const double *p) {
-        double r;
-        asm("ld.global.nc.L1::no_allocate.f64 %0, [%1];" : "=d"(r) : "l"(p));
-        return r;
-    }
-    static __device__ __forceinline__ A cached1(const double *p) { return __ldg(p); }
-};
-
-template <>
-struct VT<float> {
-    using X = float;
-    using A = float;
-    static __device__ __forceinline__ void load4(const float *p, A v[4]) {
-        asm("ld.global.nc.L1::no_allocate.v4.f32 {%0,%1,%2,%3}, [%4];"
-            : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]) : "l"(p));
-    }
-    static __device__ __forceinline__ A stream1(const float *p) {
-        float r;
-        asm("ld.global.nc.L1::no_allocate.f32 %0, [%1];" : "=f"(r) : "l"(p));
-        return r;
-    }
-    static __device__ __forceinline__ A cached1(const float *p) { return __ldg(p); }
-};
-
-template <>
-struct VT<bf16x2_t> {
-    using X = float;
-    using A = float;
-    static __device__ __forceinline__ void load4(const bf16x2_t *p, A v[4]) {
-        uint32_t u[4];
-        asm("ld.global.nc.L1::no_allocate.v4.u32 {%0,%1,%2,%3}, [%4];"
-            : "=r"(u[0]), "=r"(u[1]), "=r"(u[2]), "=r"(u[3]) : "l"(p));
-#pragma unroll
-        for (int k = 0; k < 4; k++) v[k] = bf16x2_decode(u[k]);
-    }
-    static __device__ __forceinline__ A stream1(const bf16x2_t *p) {
-        uint32_t u;
-        asm("ld.global.nc.L1::no_allocate.u32 %0, [%1];" : "=r"(u) : "l"(p));
-        return bf16x2_decode(u);
-    }
-    static __device__ __forceinline__ A cached1(const bf16x2_t *p) {
-        return bf16x2_decode(__ldg((const unsigned *)p));
-    }
-};
 
 template <typename V, typename Y>
 struct FormArgs {
@@ -103,8 +37,9 @@ struct FormArgs {
     const V *val;
     int nitems;
     // heavy band
-    int H0, nh, nslices, bulk, atomic_heavy;
-    const int *slice_ptr, *hrow, *hlen;
+    int H0, nh, nslices, nunits, bulk;
+    int heavy_mode;  // 0: atomic add, 1: y += (rows owned by one lane), 2: y = (every row owned, y not zeroed)
+    const int *slice_ptr, *hrow, *hlen, *unit_slice;
     const V *hval;
     const uint16_t *hcol16;
     const int *hcol32;
@@ -113,105 +48,6 @@ struct FormArgs {
     int *err;
     int *next;
 };
-
-// Sorted column of nonzero e of a region (see fl_stream.cuh).
-__device__ __forceinline__ int region_col(int e, const RegionDesc &rg) {
-    const int q = e - rg.start;
-    return rg.full ? rg.col_base + 32 * (q / rg.div) + (q & 31) : rg.col_base + q % rg.div;
-}
-
-// K = 1 light item: four nonzeros per lane, run merging as in process4_f64,
-// products and run sums in A, one atomic per run into Y.
-template <typename V, typename Y>
-__device__ __forceinline__ void light_item_k1(const ItemDesc &d, const RegionDesc *__restrict__ regions,
-                                              const int *__restrict__ row, const V *__restrict__ val,
-                                              const typename VT<V>::X *__restrict__ xs, Y *__restrict__ y,
-                                              int lane) {
-    using A = typename VT<V>::A;
-    const RegionDesc rg = regions[d.region];
-    for (int e = d.begin & ~3; e < d.end; e += 128) {
-        const int eb = e + 4 * lane;
-        const int4 rr = ld_stream_i4(row + eb);
-        A v[4];
-        VT<V>::load4(val + eb, v);
-        int r[4] = {rr.x, rr.y, rr.z, rr.w};
-        A p[4];
-        const int qa = eb - rg.start;
-        const int qb = qa > 0 ? qa : 0;
-        const int c0 = qb / rg.div;
-        const int r0 = qb - c0 * rg.div;
-#pragma unroll
-        for (int k = 0; k < 4; k++) {
-            const int ek = eb + k;
-            const bool valid = ek >= d.begin && ek < d.end;
-            const int delta = qa + k - qb;
-            int col;
-            if (rg.full) {
-                col = rg.col_base + 32 * (c0 + (r0 + delta >= rg.div ? 1 : 0)) + ((qa + k) & 31);
-            } else {
-                int t = r0 + delta;
-#pragma unroll
-                for (int w = 0; w < 3; w++)
-                    if (t >= rg.div) t -= rg.div;
-                col = rg.col_base + t;
-            }
-            if (valid) {
-                p[k] = v[k] * (A)__ldg(xs + col);
-            } else {
-                p[k] = (A)0;
-                r[k] = -1;
-            }
-        }
-        const bool b1 = r[1] != r[0], b2 = r[2] != r[1], b3 = r[3] != r[2];
-        const int prev_rl = __shfl_up_sync(FULLM, r[3], 1);
-        const int next_rf = __shfl_down_sync(FULLM, r[0], 1);
-        const bool cont = lane > 0 && r[0] >= 0 && prev_rl == r[0];
-        const bool cont_next = lane < 31 && r[3] >= 0 && next_rf == r[3];
-        const bool merge = (!b1 && r[0] >= 0) || (!b2 && r[1] >= 0) || (!b3 && r[2] >= 0) || cont;
-        if (!__any_sync(FULLM, merge)) {
-#pragma unroll
-            for (int k = 0; k < 4; k++)
-                if (r[k] >= 0) atomicAdd(y + r[k], (Y)p[k]);
-            continue;
-        }
-        A T = p[3];
-        if (!b3) {
-            T += p[2];
-            if (!b2) {
-                T += p[1];
-                if (!b1) T += p[0];
-            }
-        }
-        const bool full_lane = !b1 && !b2 && !b3;
-        A S = T;
-        int h = (full_lane && cont) ? 0 : 1;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const A Sn = __shfl_up_sync(FULLM, S, o);
-            const int hn = __shfl_up_sync(FULLM, h, o);
-            if (lane >= o && !h) {
-                S += Sn;
-                h = hn;
-            }
-        }
-        const A Sp = __shfl_up_sync(FULLM, S, 1);
-        const A C = cont ? Sp : (A)0;
-        A acc = p[0];
-        bool lead = true;
-        const bool brk[4] = {false, b1, b2, b3};
-#pragma unroll
-        for (int k = 1; k < 4; k++) {
-            if (brk[k]) {
-                if (r[k - 1] >= 0) atomicAdd(y + r[k - 1], (Y)(lead ? acc + C : acc));
-                acc = p[k];
-                lead = false;
-            } else {
-                acc += p[k];
-            }
-        }
-        if (!cont_next && r[3] >= 0) atomicAdd(y + r[3], (Y)S);
-    }
-}
 
 // K > 1 light item: K lanes per nonzero, lane (g, r) adds the rhs-r product
 // of nonzero e+g; a warp instruction's atomics cover 32/K rows x K
@@ -266,61 +102,95 @@ __device__ __forceinline__ void load_xk(const X *p, X out[K]) {
     }
 }
 
-// Heavy slice: lane owns one row, K sums in A.
+// Heavy unit: slices [ub, ue), lane l owns row l of each slice and keeps K
+// sums in A.  Software-pipelined over (slice, group of G entries): the next
+// group's value/column loads are issued before the current group's x gathers
+// and FMAs, so each warp keeps two groups of loads in flight.
+template <typename V, int G, bool C16, typename Y>
+__device__ __forceinline__ void heavy_load_group(const FormArgs<V, Y> &a, int base, int j0, int len, int lane,
+                                                 typename VT<V>::A v[G], int c[G]) {
+#pragma unroll
+    for (int g = 0; g < G; g++) {
+        if (j0 + g < len) {
+            const int idx = base + 32 * (j0 + g) + lane;
+            v[g] = VT<V>::stream1(a.hval + idx);
+            if constexpr (C16) c[g] = (int)__ldg(a.hcol16 + idx);
+            else c[g] = __ldg(a.hcol32 + idx);
+        }
+    }
+}
+
 template <typename V, int K, bool XS, bool C16, typename Y>
-__device__ __forceinline__ void heavy_slice(const FormArgs<V, Y> &a, int sl, const typename VT<V>::X *xsrc, int lane) {
+__device__ __forceinline__ void heavy_unit(const FormArgs<V, Y> &a, int ub, int ue, const typename VT<V>::X *xsrc,
+                                           int lane) {
     using A = typename VT<V>::A;
     using X = typename VT<V>::X;
-    const int base = __ldg(a.slice_ptr + sl);
-    const int w = (__ldg(a.slice_ptr + sl + 1) - base) >> 5;
-    const int r = __ldg(a.hrow + 32 * sl + lane), len = __ldg(a.hlen + 32 * sl + lane);
+    constexpr int G = K == 1 ? (sizeof(A) == 8 ? 4 : 8) : (sizeof(A) == 8 ? 1 : 2);
+    if (ub >= ue) return;
+    int sl = ub;
+    int base = __ldg(a.slice_ptr + sl);
+    int w = (__ldg(a.slice_ptr + sl + 1) - base) >> 5;
+    int r = __ldg(a.hrow + 32 * sl + lane), len = __ldg(a.hlen + 32 * sl + lane);
+    int j0 = 0;
+    A v[G];
+    int c[G];
+    heavy_load_group<V, G, C16, Y>(a, base, j0, len, lane, v, c);
     A acc[K];
 #pragma unroll
     for (int q = 0; q < K; q++) acc[q] = (A)0;
-    const V *vp = a.hval + base + lane;
-    constexpr int UNR = K == 1 ? 4 : 2;
-    int j = 0;
-    for (; j + UNR <= w; j += UNR) {
-        A v[UNR];
-        int c[UNR];
-#pragma unroll
-        for (int k = 0; k < UNR; k++) {
-            if (j + k < len) {
-                v[k] = VT<V>::stream1(vp + 32 * (j + k));
-                if constexpr (C16) c[k] = (int)__ldg(a.hcol16 + base + 32 * (j + k) + lane);
-                else c[k] = __ldg(a.hcol32 + base + 32 * (j + k) + lane);
+    for (;;) {
+        int nsl = sl, nj0 = j0 + G, nbase = base, nw = w, nr = r, nlen = len;
+        if (nj0 >= w) {
+            nsl = sl + 1;
+            nj0 = 0;
+            if (nsl < ue) {
+                nbase = __ldg(a.slice_ptr + nsl);
+                nw = (__ldg(a.slice_ptr + nsl + 1) - nbase) >> 5;
+                nr = __ldg(a.hrow + 32 * nsl + lane);
+                nlen = __ldg(a.hlen + 32 * nsl + lane);
             }
         }
+        const bool has_next = nsl < ue;
+        A nv[G];
+        int nc[G];
+        if (has_next) heavy_load_group<V, G, C16, Y>(a, nbase, nj0, nlen, lane, nv, nc);
 #pragma unroll
-        for (int k = 0; k < UNR; k++) {
-            if (j + k < len) {
+        for (int g = 0; g < G; g++) {
+            if (j0 + g < len) {
                 X xv[K];
-                load_xk<X, K, XS>(xsrc + (size_t)c[k] * K, xv);
+                load_xk<X, K, XS>(xsrc + (size_t)c[g] * K, xv);
 #pragma unroll
-                for (int q = 0; q < K; q++) acc[q] = fma(v[k], (A)xv[q], acc[q]);
+                for (int q = 0; q < K; q++) acc[q] = fma(v[g], (A)xv[q], acc[q]);
             }
         }
-    }
-    for (; j < w; j++) {
-        if (j < len) {
-            const A v = VT<V>::stream1(vp + 32 * j);
-            int c;
-            if constexpr (C16) c = (int)__ldg(a.hcol16 + base + 32 * j + lane);
-            else c = __ldg(a.hcol32 + base + 32 * j + lane);
-            X xv[K];
-            load_xk<X, K, XS>(xsrc + (size_t)c * K, xv);
+        if (nsl != sl) {
+            if (len > 0) {
+                Y *yr = a.y + (size_t)r * K;
+                if (a.heavy_mode == 0) {
 #pragma unroll
-            for (int q = 0; q < K; q++) acc[q] = fma(v, (A)xv[q], acc[q]);
+                    for (int q = 0; q < K; q++) atomicAdd(yr + q, (Y)acc[q]);
+                } else if (a.heavy_mode == 1) {
+#pragma unroll
+                    for (int q = 0; q < K; q++) yr[q] += (Y)acc[q];
+                } else {
+#pragma unroll
+                    for (int q = 0; q < K; q++) yr[q] = (Y)acc[q];
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < K; q++) acc[q] = (A)0;
         }
-    }
-    if (len > 0) {
-        Y *yr = a.y + (size_t)r * K;
-        if (a.atomic_heavy) {
+        if (!has_next) break;
+        sl = nsl;
+        j0 = nj0;
+        base = nbase;
+        w = nw;
+        r = nr;
+        len = nlen;
 #pragma unroll
-            for (int q = 0; q < K; q++) atomicAdd(yr + q, (Y)acc[q]);
-        } else {
-#pragma unroll
-            for (int q = 0; q < K; q++) yr[q] += (Y)acc[q];
+        for (int g = 0; g < G; g++) {
+            v[g] = nv[g];
+            c[g] = nc[g];
         }
     }
 }
@@ -363,7 +233,7 @@ __global__ void __launch_bounds__(FM_THREADS, 1) k_spmv_form(const FormArgs<V, Y
         }
     }
     const X *xsrc = XS ? (const X *)xh : a.xs + (size_t)a.H0 * K;
-    const int total = a.nitems + (use_band ? a.nslices : 0);
+    const int total = a.nitems + (use_band ? a.nunits : 0);
     bool staged = !(XS && use_band && a.bulk);
     for (;;) {
         int u = 0;
@@ -371,7 +241,7 @@ __global__ void __launch_bounds__(FM_THREADS, 1) k_spmv_form(const FormArgs<V, Y
         u = __shfl_sync(FULLM, u, 0);
         if (u >= total) break;
         if (u < a.nitems) {
-            if constexpr (K == 1) light_item_k1<V, Y>(a.items[u], a.regions, a.row, a.val, a.xs, a.y, lane);
+            if constexpr (K == 1) stream_item<V, Y, 1>(a.items[u], a.regions, a.row, a.val, a.xs, a.y, lane);
             else light_item_kn<V, K, Y>(a.items[u], a.regions, a.row, a.val, a.xs, a.y, lane);
             continue;
         }
@@ -393,7 +263,8 @@ __global__ void __launch_bounds__(FM_THREADS, 1) k_spmv_form(const FormArgs<V, Y
             }
             staged = true;
         }
-        heavy_slice<V, K, XS, C16, Y>(a, u - a.nitems, xsrc, lane);
+        heavy_unit<V, K, XS, C16, Y>(a, __ldg(a.unit_slice + (u - a.nitems)), __ldg(a.unit_slice + (u - a.nitems) + 1),
+                                     xsrc, lane);
     }
     if (XS && use_band && a.bulk && !staged) {
         bool ok = false;
@@ -419,7 +290,7 @@ int launch_form(const FormArgs<V, Y> &a, size_t smem, cudaStream_t s) {
     int per_sm = 0;
     FL_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, FM_THREADS, smem));
     if (per_sm <= 0) per_sm = 1;
-    const long units = (long)a.nitems + a.nslices;
+    const long units = (long)a.nitems + a.nunits;
     const long grid = std::max<long>(1, std::min<long>((long)num_sms() * per_sm, (units + 31) / 32));
     kern<<<(int)grid, FM_THREADS, smem, s>>>(a);
     FL_CUDA(cudaGetLastError());

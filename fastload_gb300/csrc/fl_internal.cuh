@@ -139,6 +139,8 @@ struct HeavyBand {
     DevBuf<int> slice_ptr;      // nslices+1
     DevBuf<int> row;            // 32*nslices, -1 for an empty lane
     DevBuf<int> len;            // 32*nslices
+    int nunits = 0;             // work units: runs of consecutive slices
+    DevBuf<int> unit_slice;     //   (nunits+1 bounds)
 };
 
 // Bucketed form: light columns [0, H0) keep the FastLoad tile stream, the

@@ -9,16 +9,13 @@
 //    per-tile arrays (tile_ptr/len/colidx/format, sortrowindex) -- the
 //    reference's kernel design, rebuilt for CUDA 13 with its defects fixed
 //    (in-bounds loads, _sync shuffles, one product per lane).
-//  * k_spmv_stream_f64: the streaming kernel.  It reads no per-tile metadata:
-//    the tile-ordered value/row streams are cut into work items, each lane
-//    takes four consecutive nonzeros with 128-bit loads, derives each one's
-//    sorted column arithmetically from the step table (full 32-wide chunks:
-//    col = col_base + 32*(q / (32*tall)) + q%32; partial chunk:
-//    col = col_base + q % len) and gathers x through L1.  Runs of equal rows
-//    are merged by a warp-wide segmented scan over the 128-nonzero block
-//    (__shfl_sync), skipped when a ballot shows the block has none, so the
-//    common case spends exactly one FP64 multiply per nonzero -- GB300's FP64
-//    pipe is narrow and would otherwise bound the kernel.
+//  * k_spmv_stream_f64: the streaming kernel (fl_stream.cuh).  It reads no
+//    per-tile metadata: the tile-ordered value/row streams are cut into work
+//    items walked 32 nonzeros per warp row, each nonzero's sorted column
+//    derived arithmetically from the step table, x gathered through L1, runs
+//    of equal rows merged by a segmented shuffle scan only when present -- so
+//    the common case spends exactly one FP64 multiply per nonzero (GB300's
+//    FP64 pipe is narrow and would otherwise bound the kernel).
 #include "fl_stream.cuh"
 
 namespace fl {
@@ -32,7 +29,7 @@ __global__ void __launch_bounds__(256) k_spmv_stream_f64(const ItemDesc *__restr
     const int lane = threadIdx.x & 31;
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
-    for (int it = gw; it < nitems; it += nw) stream_item_f64<U>(items[it], regions, row, val, xs, y, lane);
+    for (int it = gw; it < nitems; it += nw) stream_item<double, double, U>(items[it], regions, row, val, xs, y, lane);
 }
 
 // One warp per reference tile (FastLoad_GPU.h:170-271): format 0 tiles add

@@ -1,8 +1,19 @@
-// fl_stream.cuh -- device side of the FastLoad streaming SpMV: 128-bit
-// stream loads, per-nonzero column derivation from a region descriptor, and
-// the run-merging warp reduction with one FP64 atomic per run.  Shared by the
-// streaming kernel (fl_spmv.cu) and the light part of the bucketed kernel
-// (fl_bucket.cu).
+// fl_stream.cuh -- device side of the FastLoad streaming SpMV, shared by the
+// plain streaming kernel (fl_spmv.cu), the light part of the bucketed kernel
+// (fl_bucket.cu) and the storage forms (fl_forms.cuh).
+//
+// A warp walks a work item 32 nonzeros at a time: lane l takes nonzero
+// e + 32k + l (k = 0..4U-1 per iteration), so every load of a 32-nonzero row
+// is one coalesced 128-byte (rows) / 256-byte (FP64 values) request and, when
+// a tile's rows are consecutive (banded matrices), every atomic instruction
+// covers 8 sectors instead of 32.  The sorted column of each nonzero follows
+// from the region descriptor with one division per lane per iteration:
+// in a full region (32-wide chunks of `tall` levels) col = col_base +
+// 32*(q / 32*tall) + q%32 and q%32 is the same for all of a lane's nonzeros;
+// in a partial chunk col = col_base + q % len.  Runs of equal consecutive
+// rows inside each 32-nonzero row are summed by a segmented shuffle scan
+// (only when a ballot finds one) and added to y once per run -- the run
+// semantics of the reference's tile formats 1/2 (FastLoad_GPU.h:192-270).
 #pragma once
 
 #include "fl_internal.cuh"
@@ -11,135 +22,154 @@ namespace fl {
 
 constexpr unsigned FULLM = 0xffffffffu;
 
-__device__ __forceinline__ int4 ld_stream_i4(const int *p) {
-    int4 r;
-    asm("ld.global.nc.L1::no_allocate.v4.s32 {%0,%1,%2,%3}, [%4];"
-        : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w)
-        : "l"(p));
-    return r;
+struct bf16x2_t {
+    uint32_t u;
+};
+
+__device__ __forceinline__ float bf16x2_decode(uint32_t u) {
+    return __uint_as_float(u << 16) + __uint_as_float(u & 0xffff0000u);
 }
-__device__ __forceinline__ double2 ld_stream_d2(const double *p) {
-    double2 r;
-    asm("ld.global.nc.L1::no_allocate.v2.f64 {%0,%1}, [%2];" : "=d"(r.x), "=d"(r.y) : "l"(p));
+
+__device__ __forceinline__ int ld_stream_i32(const int *p) {
+    int r;
+    asm("ld.global.nc.L1::no_allocate.s32 %0, [%1];" : "=r"(r) : "l"(p));
     return r;
 }
 
-// Four consecutive nonzeros of one lane: products, run merging, atomics.
-__device__ __forceinline__ void process4_f64(int eb, int4 rr, double2 va, double2 vb, const ItemDesc &d,
-                                             const RegionDesc &rg, const double *__restrict__ xs,
-                                             double *__restrict__ y, int lane) {
-    int r[4] = {rr.x, rr.y, rr.z, rr.w};
-    const double v[4] = {va.x, va.y, vb.x, vb.y};
-    double p[4];
-    // sorted column of each nonzero; one division per lane
-    int qa = eb - rg.start;
-    int qb = qa > 0 ? qa : 0;
-    int c0 = qb / rg.div;
-    int r0 = qb - c0 * rg.div;
-#pragma unroll
-    for (int k = 0; k < 4; k++) {
-        int e = eb + k;
-        bool valid = e >= d.begin && e < d.end;
-        int delta = qa + k - qb;  // >= 0 whenever valid
-        int col;
-        if (rg.full) {
-            int c = c0 + (r0 + delta >= rg.div ? 1 : 0);
-            col = rg.col_base + 32 * c + ((qa + k) & 31);
-        } else {
-            int t = r0 + delta;
-#pragma unroll
-            for (int w = 0; w < 3; w++)
-                if (t >= rg.div) t -= rg.div;
-            col = rg.col_base + t;
-        }
-        if (valid) {
-            p[k] = v[k] * __ldg(xs + col);
-        } else {
-            p[k] = 0.0;
-            r[k] = -1;
-        }
+// Value storage traits: X = x type, A = arithmetic type of products and sums.
+template <typename V>
+struct VT;
+
+template <>
+struct VT<double> {
+    using X = double;
+    using A = double;
+    static __device__ __forceinline__ A stream1(const double *p) {
+        double r;
+        asm("ld.global.nc.L1::no_allocate.f64 %0, [%1];" : "=d"(r) : "l"(p));
+        return r;
     }
-    const bool b1 = r[1] != r[0], b2 = r[2] != r[1], b3 = r[3] != r[2];
-    const int rf = r[0], rl = r[3];
-    const int prev_rl = __shfl_up_sync(FULLM, rl, 1);
-    const int next_rf = __shfl_down_sync(FULLM, rf, 1);
-    const bool cont = lane > 0 && rf >= 0 && prev_rl == rf;
-    const bool cont_next = lane < 31 && rl >= 0 && next_rf == rl;
-    const bool merge = (!b1 && r[0] >= 0) || (!b2 && r[1] >= 0) || (!b3 && r[2] >= 0) || cont;
-    if (!__any_sync(FULLM, merge)) {
-#pragma unroll
-        for (int k = 0; k < 4; k++)
-            if (r[k] >= 0) atomicAdd(y + r[k], p[k]);
+    static __device__ __forceinline__ A cached1(const double *p) { return __ldg(p); }
+};
+
+template <>
+struct VT<float> {
+    using X = float;
+    using A = float;
+    static __device__ __forceinline__ A stream1(const float *p) {
+        float r;
+        asm("ld.global.nc.L1::no_allocate.f32 %0, [%1];" : "=f"(r) : "l"(p));
+        return r;
+    }
+    static __device__ __forceinline__ A cached1(const float *p) { return __ldg(p); }
+};
+
+template <>
+struct VT<bf16x2_t> {
+    using X = float;
+    using A = float;
+    static __device__ __forceinline__ A stream1(const bf16x2_t *p) {
+        uint32_t u;
+        asm("ld.global.nc.L1::no_allocate.u32 %0, [%1];" : "=r"(u) : "l"(p));
+        return bf16x2_decode(u);
+    }
+    static __device__ __forceinline__ A cached1(const bf16x2_t *p) {
+        return bf16x2_decode(__ldg((const unsigned *)p));
+    }
+};
+
+// y[r] += p for one 32-nonzero row of the stream (r = -1: no nonzero).
+template <typename A, typename Y>
+__device__ __forceinline__ void emit_row32(int r, A p, Y *__restrict__ y, int lane) {
+    const int prev = __shfl_up_sync(FULLM, r, 1);
+    const bool join = lane > 0 && r >= 0 && prev == r;
+    if (!__any_sync(FULLM, join)) {
+        if (r >= 0) atomicAdd(y + r, (Y)p);
         return;
     }
-    // Trailing-run sum of the lane, then a segmented inclusive scan across
-    // lanes: a lane continues the previous segment when all four of its
-    // nonzeros are one run that started in an earlier lane.
-    double T = p[3];
-    if (!b3) {
-        T += p[2];
-        if (!b2) {
-            T += p[1];
-            if (!b1) T += p[0];
-        }
-    }
-    const bool full_lane = !b1 && !b2 && !b3;
-    double S = T;
-    int h = (full_lane && cont) ? 0 : 1;
+    A S = p;
+    int h = join ? 0 : 1;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-        double Sn = __shfl_up_sync(FULLM, S, o);
-        int hn = __shfl_up_sync(FULLM, h, o);
+        const A Sn = __shfl_up_sync(FULLM, S, o);
+        const int hn = __shfl_up_sync(FULLM, h, o);
         if (lane >= o && !h) {
             S += Sn;
             h = hn;
         }
     }
-    const double Sp = __shfl_up_sync(FULLM, S, 1);
-    const double C = cont ? Sp : 0.0;
-    // runs ending inside the lane emit here; the lane's leading run adds the
-    // carry from earlier lanes; the trailing run emits unless the next lane
-    // continues it.
-    double acc = p[0];
-    bool lead = true;
-    const bool brk[4] = {false, b1, b2, b3};
-#pragma unroll
-    for (int k = 1; k < 4; k++) {
-        if (brk[k]) {
-            if (r[k - 1] >= 0) atomicAdd(y + r[k - 1], lead ? acc + C : acc);
-            acc = p[k];
-            lead = false;
-        } else {
-            acc += p[k];
-        }
-    }
-    if (!cont_next && r[3] >= 0) atomicAdd(y + r[3], S);
+    const int next = __shfl_down_sync(FULLM, r, 1);
+    if ((lane == 31 || next != r) && r >= 0) atomicAdd(y + r, (Y)S);
 }
 
-// One work item: 128*U nonzeros per warp iteration, loads of the U blocks
-// issued before any of them is processed.
-template <int U>
-__device__ __forceinline__ void stream_item_f64(const ItemDesc &d, const RegionDesc *__restrict__ regions,
-                                                const int *__restrict__ row, const double *__restrict__ val,
-                                                const double *__restrict__ xs, double *__restrict__ y,
-                                                int lane) {
+// One work item; 4U rows of 32 nonzeros per warp iteration, all loads of an
+// iteration issued before any is used.
+template <typename V, typename Y, int U>
+__device__ __forceinline__ void stream_item(const ItemDesc &d, const RegionDesc *__restrict__ regions,
+                                            const int *__restrict__ row, const V *__restrict__ val,
+                                            const typename VT<V>::X *__restrict__ xs, Y *__restrict__ y,
+                                            int lane) {
+    using A = typename VT<V>::A;
+    constexpr int R = 4 * U;
     const RegionDesc rg = regions[d.region];
-    for (int e = d.begin & ~3; e < d.end; e += 128 * U) {
-        int4 rr[U];
-        double2 va[U], vb[U];
+    const int div = rg.div;
+    const int s32 = rg.full ? 0 : 32 % div;  // partial chunk: column step per 32 nonzeros
+    for (int e = d.begin & ~31; e < d.end; e += 32 * R) {
+        const int el0 = e + lane;
+        int rw[R];
+        A v[R];
 #pragma unroll
-        for (int u = 0; u < U; u++) {
-            const int eb = e + 128 * u + 4 * lane;
-            rr[u] = ld_stream_i4(row + eb);
-            va[u] = ld_stream_d2(val + eb);
-            vb[u] = ld_stream_d2(val + eb + 2);
+        for (int k = 0; k < R; k++) {
+            rw[k] = ld_stream_i32(row + el0 + 32 * k);
+            v[k] = VT<V>::stream1(val + el0 + 32 * k);
+        }
+        // columns of the lane's R nonzeros (they do not depend on the loads,
+        // so every x gather is issued before any loaded value is used)
+        const int q0 = el0 - rg.start;             // >= -31: items never start before their region
+        const int k0 = q0 < 0 ? 1 : 0;
+        const int qs = q0 + 32 * k0;
+        int c = qs / div;
+        int t = qs - c * div;
+        const int lo = q0 & 31;
+        // in a full region consecutive rows of a lane often share a column
+        // (levels of one chunk): gather x only where the column changes
+        typename VT<V>::X xv[R];
+        bool fresh[R];
+        int cprev = -1;
+#pragma unroll
+        for (int k = 0; k < R; k++) {
+            if (k > k0) {  // advance the column state by 32 nonzeros
+                if (rg.full) {
+                    t += 32;
+                    if (t >= div) { t -= div; c++; }
+                } else {
+                    t += s32;
+                    if (t >= div) t -= div;
+                }
+            }
+            const int el = el0 + 32 * k;
+            const bool valid = el >= d.begin && el < d.end;
+            const int col = rg.full ? rg.col_base + 32 * c + lo : rg.col_base + t;
+            fresh[k] = valid && (!rg.full || c != cprev);
+            if (fresh[k]) {
+                xv[k] = __ldg(xs + col);
+                cprev = c;
+            }
         }
 #pragma unroll
-        for (int u = 0; u < U; u++) {
-            const int eb = e + 128 * u + 4 * lane;
-            process4_f64(eb, rr[u], va[u], vb[u], d, rg, xs, y, lane);
+        for (int k = 0; k < R; k++) {
+            const int el = el0 + 32 * k;
+            const bool valid = el >= d.begin && el < d.end;
+            if (k > 0 && !fresh[k]) xv[k] = xv[k - 1];
+            emit_row32<A, Y>(valid ? rw[k] : -1, valid ? v[k] * (A)xv[k] : (A)0, y, lane);
         }
     }
+}
+
+// Sorted column of nonzero e of a region.
+__device__ __forceinline__ int region_col(int e, const RegionDesc &rg) {
+    const int q = e - rg.start;
+    return rg.full ? rg.col_base + 32 * (q / rg.div) + (q & 31) : rg.col_base + q % rg.div;
 }
 
 }  // namespace fl
