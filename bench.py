@@ -272,6 +272,57 @@ def measure_forms(fl, peak, reps=30):
     return out
 
 
+def measure_batch(fl, peak, reps=10):
+    """Batched form: 256 independent seeded matrices (n log-uniform in
+    [1e3, 2e5], mean degree U[4, 32], half Poisson and half Zipf(1.5) column
+    degrees), FP32 values with FP32 accumulation, one persistent launch,
+    direct and replayed from a captured CUDA graph; against the plain FP64
+    streaming kernel launched once per matrix on the same inputs."""
+    import torch
+
+    import oracle
+    from fastload_gb300 import gen
+
+    mats = gen.batch(256, seed=3, dtype=np.float64)
+    flush = torch.empty(64 << 20, dtype=torch.float32, device="cuda")
+    t0 = time.perf_counter()
+    plans = [fl.Plan.from_csc(c.m, c.n, c.colptr, c.rowidx, c.val, heavy_band=-1) for c in mats]
+    prep = time.perf_counter() - t0
+    nnz = sum(c.nnz for c in mats)
+    M, N = sum(c.m for c in mats), sum(c.n for c in mats)
+    x = torch.from_numpy(np.concatenate([c.x for c in mats])).cuda()
+    out = {"matrices": len(mats), "nnz": nnz, "rows": M, "plan_build_s": prep}
+    # plain FP64 kernel, one launch per matrix
+    xs64 = [p.permute_x(torch.from_numpy(c.x).cuda()) for p, c in zip(plans, mats)]
+    ys64 = [torch.empty(c.m, dtype=torch.float64, device="cuda") for c in mats]
+
+    def plain():
+        for p, xs_, y_ in zip(plans, xs64, ys64):
+            p.spmv(xs_, y_, kernel=fl.KERNEL_STREAM2)
+
+    t_plain = _time_ms(plain, reps, flush)
+    out["plain_fp64_per_matrix"] = {"ms": t_plain, "gflops": 2.0 * nnz / (t_plain * 1e-3) / 1e9, "launches": len(mats)}
+    with fl.Batch(plans, value_type=fl.VALUES_F32, y_f32=True) as b:
+        for p in plans:
+            p.close()
+        xs = b.permute_x(x)
+        y = torch.empty(b.m, dtype=torch.float32, device="cuda")
+        t_direct = _time_ms(lambda: b.spmv(xs, y), reps, flush)
+        t_graph = _time_ms(lambda: b.spmv_graph(xs, y), reps, flush)
+        yh = y.double().cpu().numpy()
+    worst = 0.0
+    for i, c in enumerate(mats):
+        ref = oracle.csc_spmv_dd(c.m, c.n, c.colptr, c.rowidx, c.val, c.x)
+        nw, _ = oracle.rel_errors(yh[b.m_off[i]:b.m_off[i + 1]], ref)
+        worst = max(worst, nw)
+    Bf = nnz * 8 + (N + len(mats)) * 4 + N * 4 + M * 4
+    for name, t in (("batch_fp32_direct", t_direct), ("batch_fp32_graph", t_graph)):
+        out[name] = {"ms": t, "gbs": Bf / (t * 1e-3) / 1e9, "pct_of_peak": 100.0 * Bf / (t * 1e-3) / 1e9 / peak,
+                     "gflops": 2.0 * nnz / (t * 1e-3) / 1e9, "launches": 1,
+                     "gflops_vs_plain_fp64": t_plain / t, "rel_err_normwise_worst_matrix": worst}
+    return out
+
+
 def run_profile(spec):
     """--profile case:values:band:k -- builds one case and runs one kernel a
     few times (for ncu captures).  case lap128 | zipf | zipf<n>; values
@@ -409,6 +460,7 @@ def run_gpu(args, rank, world):
 
     peak, peak_kind = measured_peaks()
     forms = measure_forms(fl, peak) if (rank == 0 and not args.quick and not args.no_forms) else None
+    batch = measure_batch(fl, peak) if (rank == 0 and not args.quick and not args.no_forms) else None
     if rank != 0:
         if dist:
             dist.destroy_process_group()
@@ -434,6 +486,7 @@ def run_gpu(args, rank, world):
         "speedup_vs_plain_fp64_stream": (variants["stream2"] and achieved / variants["stream2"]) if variants else None,
         "preprocess_s": prep_s,
         "forms": forms,
+        "batch": batch,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_kind": f"{peak_kind} hbm_gbs",
                      "kernel": kname, "bytes_per_launch": B, "kernel_ms": kern_ms},

@@ -86,6 +86,14 @@ SIGNATURES = [
     ("fl_plan_form_info", C.c_int, [C.c_void_p, C.c_int, C.POINTER(FormInfoC)]),
     ("fl_plan_spmv_form", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
     ("fl_plan_permute_x_k", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("fl_batch_create", C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.POINTER(C.c_void_p), C.c_int, C.c_int]),
+    ("fl_batch_info", C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_long), C.POINTER(C.c_long),
+                                C.POINTER(C.c_long), C.POINTER(C.c_int)]),
+    ("fl_batch_offsets", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("fl_batch_permute_x", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("fl_batch_spmv", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("fl_batch_spmv_graph", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("fl_batch_destroy", C.c_int, [C.c_void_p]),
     ("fl_col_sort_noalloc", C.c_int, [C.c_int, C.c_int] + [C.c_void_p] * 11),
 ]
 

@@ -66,17 +66,35 @@ def _distinct_rows(rng: np.random.Generator, m: int, deg: np.ndarray, forced_row
     forced row of c when given).  Returns sorted int64 keys col*m + row."""
     n = deg.size
     deg = np.minimum(deg.astype(np.int64), m)
+    # dense columns (a quarter of the rows or more) are drawn exactly, the
+    # rest by vectorised rejection of duplicates
+    dense = np.flatnonzero(deg * 4 >= m) if m > 0 else np.zeros(0, np.int64)
+    dense_keys = []
+    for c in dense:
+        rows = rng.choice(m, size=int(deg[c]), replace=False).astype(np.int64)
+        if forced_rows is not None and forced_rows[c] not in rows:
+            rows[0] = forced_rows[c]
+        dense_keys.append(c * m + rows)
+    if dense.size:
+        deg = deg.copy()
+        deg[dense] = 0
     target = deg.copy()
+    if forced_rows is not None:
+        forced_rows = np.asarray(forced_rows, np.int64).copy()
     cols = np.repeat(np.arange(n, dtype=np.int64), deg)
     keys = cols * m + rng.integers(0, m, size=cols.size)
     if forced_rows is not None:
-        keys = np.concatenate([keys, np.arange(n, dtype=np.int64) * m + forced_rows])
-        target = np.minimum(target + 1, m)
+        sparse = np.ones(n, bool)
+        sparse[dense] = False
+        keys = np.concatenate([keys, np.flatnonzero(sparse).astype(np.int64) * m + forced_rows[sparse]])
+        target = np.where(sparse, np.minimum(target + 1, m), 0)
     keys = _sorted_unique(keys)
-    for _ in range(64):
+    for _ in range(256):
         cnt = np.bincount(keys // m, minlength=n)
         deficit = target - cnt
         if not deficit.any():
+            if dense_keys:
+                keys = np.sort(np.concatenate([keys] + dense_keys))
             return keys
         # over-full columns (forced row drawn twice can't happen: unique) are
         # impossible; draw more for the short ones

@@ -230,6 +230,32 @@ int fl_plan_spmv_form(fl_plan_t plan, int form_id, int k, const void *d_xs,
 int fl_plan_permute_x_k(fl_plan_t plan, int k, int to_f32, const double *d_x,
                         void *d_xs, void *stream);
 
+/* ---- batches: many matrices, one persistent launch ---------------------- */
+
+typedef struct fl_batch *fl_batch_t;
+
+/* Stacks the FastLoad layouts of `count` plans (which may be destroyed
+ * afterwards) into one work list: y and x of the matrices are stacked in
+ * plan order (offsets from fl_batch_offsets), values stored as value_type,
+ * y accumulated in FP32 when y_f32 (FP32 values only) else FP64. */
+int fl_batch_create(fl_batch_t *batch, int count, const fl_plan_t *plans,
+                    int value_type, int y_f32);
+int fl_batch_info(fl_batch_t batch, int *count, long *m_total, long *n_total,
+                  long *nnz_total, int *items);
+/* m_off, n_off: count+1 entries each (stacked row / column offsets). */
+int fl_batch_offsets(fl_batch_t batch, int *m_off, int *n_off);
+/* Stacked x in original column order -> stacked sorted x (float unless the
+ * batch stores FP64 values). */
+int fl_batch_permute_x(fl_batch_t batch, const double *d_x, void *d_xs,
+                       void *stream);
+/* y = A xs for every matrix of the batch in one launch (asynchronous). */
+int fl_batch_spmv(fl_batch_t batch, const void *d_xs, void *d_y, void *stream);
+/* The same through a CUDA graph captured on the first call (and again when
+ * d_xs or d_y change) and replayed on `stream`. */
+int fl_batch_spmv_graph(fl_batch_t batch, const void *d_xs, void *d_y,
+                        void *stream);
+int fl_batch_destroy(fl_batch_t batch);
+
 /* ---- allocation-free column sort -------------------------------------- */
 
 /* Largest column count fl_col_sort_noalloc accepts (its scratch array holds

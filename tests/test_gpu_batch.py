@@ -1,0 +1,62 @@
+"""Batches: many matrices of uneven size in one persistent launch, direct and
+replayed through a captured CUDA graph, against the compensated FP64 oracle.
+
+Tolerance (normwise, per matrix): FP64 values 1e-12; FP32 values with FP64 y
+1e-6; FP32 values with FP32 accumulation into FP32 y 5e-6 (y rounding plus
+unordered FP32 atomic additions)."""
+import numpy as np
+import pytest
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def _mats(count=20, seed=21):
+    from fastload_gb300 import gen
+
+    ms = gen.batch(count, seed=seed, nmin=64, nmax=4000, dtype=np.float64)
+    ms.append(gen.from_csr_lists(5, 7, [], x=np.ones(7)))  # an empty matrix in the stack
+    return ms
+
+
+@pytest.mark.parametrize("vtype,y_f32,tol", [(0, False, 1e-12), (1, False, 1e-6), (1, True, 5e-6), (2, False, 2e-5)])
+def test_batch_matches_oracle(gpu, vtype, y_f32, tol):
+    import torch
+
+    mats = _mats()
+    plans = [gpu.Plan.from_csc(c.m, c.n, c.colptr, c.rowidx, c.val, heavy_band=-1) for c in mats]
+    with gpu.Batch(plans, value_type=vtype, y_f32=y_f32) as b:
+        for p in plans:
+            p.close()  # the batch keeps its own copy
+        assert b.count == len(mats) and b.nnz == sum(c.nnz for c in mats)
+        x = torch.from_numpy(np.concatenate([c.x for c in mats])).cuda()
+        xs = b.permute_x(x)
+        y1 = b.spmv(xs).double().cpu().numpy()
+        y2 = b.spmv_graph(xs).double().cpu().numpy()
+        y3 = b.spmv_graph(xs).double().cpu().numpy()  # replay
+        yo = torch.empty(b.m, dtype=torch.float32 if y_f32 else torch.float64, device="cuda")
+        y4 = b.spmv_graph(xs, yo).double().cpu().numpy()  # new y pointer: recapture
+        for yy in (y1, y2, y3, y4):
+            for i, c in enumerate(mats):
+                ref = oracle.csc_spmv_dd(c.m, c.n, c.colptr, c.rowidx, c.val, c.x)
+                got = yy[b.m_off[i]:b.m_off[i + 1]]
+                if c.nnz == 0:
+                    assert not got.any()
+                    continue
+                nw, mx = oracle.rel_errors(got, ref)
+                assert nw <= tol, (i, nw, mx)
+
+
+def test_batch_rejects_bad_arguments(gpu):
+    from fastload_gb300 import _lib
+
+    lib = _lib.load()
+    import ctypes as C
+
+    h = C.c_void_p()
+    assert lib.fl_batch_create(C.byref(h), 1, None, 1, 1) == -1
+    mats = _mats(2)
+    plans = [gpu.Plan.from_csc(c.m, c.n, c.colptr, c.rowidx, c.val) for c in mats]
+    with pytest.raises(gpu.FastLoadError):
+        gpu.Batch(plans, value_type=2, y_f32=True)
