@@ -94,6 +94,17 @@ SIGNATURES = [
     ("fl_batch_spmv", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("fl_batch_spmv_graph", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("fl_batch_destroy", C.c_int, [C.c_void_p]),
+    ("fl_gen_fill", C.c_int, [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double,
+                              C.c_ulonglong, C.c_void_p]),
+    ("fl_plan_features", C.c_int, [C.c_void_p, C.c_int, c_float_p]),
+    ("fl_mlp_create", C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.c_int, C.c_int, C.c_int, C.c_ulonglong]),
+    ("fl_mlp_num_params", C.c_long, [C.c_void_p]),
+    ("fl_mlp_get_params", C.c_int, [C.c_void_p, c_float_p]),
+    ("fl_mlp_set_params", C.c_int, [C.c_void_p, c_float_p]),
+    ("fl_mlp_forward", C.c_int, [C.c_void_p, c_float_p, C.c_int, c_float_p]),
+    ("fl_mlp_grad", C.c_int, [C.c_void_p, c_float_p, c_float_p, c_float_p, C.c_int, c_float_p, c_float_p]),
+    ("fl_mlp_train", C.c_int, [C.c_void_p, c_float_p, c_float_p, c_float_p, C.c_int, C.c_int, C.c_float, c_float_p]),
+    ("fl_mlp_destroy", C.c_int, [C.c_void_p]),
     ("fl_col_sort_noalloc", C.c_int, [C.c_int, C.c_int] + [C.c_void_p] * 11),
 ]
 

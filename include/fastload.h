@@ -256,6 +256,42 @@ int fl_batch_spmv_graph(fl_batch_t batch, const void *d_xs, void *d_y,
                         void *stream);
 int fl_batch_destroy(fl_batch_t batch);
 
+/* ---- tuner: synthetic matrices, features, network ----------------------- */
+
+/* Fills rows and values of a device CSC whose column pointer (degrees) the
+ * caller chose: family 0 uniform rows, 1 uniform rows (Zipf degrees), 2
+ * banded (window of `param` rows about the diagonal), 3 block-diagonal
+ * (blocks of `param`), 4 row-skewed (row = m u^param).  Rows ascend within a
+ * column (repeats possible when a degree nears its window); values uniform
+ * in [-1, 1).  Deterministic in seed. */
+int fl_gen_fill(int family, int m, int n, const int *d_colptr, int *d_rowidx,
+                double *d_val, double param, unsigned long long seed,
+                void *stream);
+/* 24 features of the plan's matrix (log sizes, column-degree moments and
+ * log2 histogram, nonzero share of the densest 2048/8192/24576 columns,
+ * distance from the diagonal, row-degree spread, value type). */
+int fl_plan_features(fl_plan_t plan, int value_type, float *out24);
+
+typedef struct fl_mlp *fl_mlp_t;
+/* MLP in -> h1 -> h2 -> out, ReLU hidden layers, He-uniform init from seed. */
+int fl_mlp_create(fl_mlp_t *mlp, int in, int h1, int h2, int out,
+                  unsigned long long seed);
+long fl_mlp_num_params(fl_mlp_t mlp);
+/* Parameters flat: W1 (in x h1, row-major), b1, W2, b2, W3, b3. */
+int fl_mlp_get_params(fl_mlp_t mlp, float *params);
+int fl_mlp_set_params(fl_mlp_t mlp, const float *params);
+/* Host buffers: X (B x in), Y (B x out). */
+int fl_mlp_forward(fl_mlp_t mlp, const float *X, int B, float *Y);
+/* Masked mean-squared error against T (mask M, NULL = all ones) and its
+ * gradient with respect to every parameter (flat, same order). */
+int fl_mlp_grad(fl_mlp_t mlp, const float *X, const float *T, const float *M,
+                int B, float *loss, float *grad);
+/* `epochs` full-batch Adam steps on the GPU; losses[e] gets each epoch's
+ * loss (may be NULL). */
+int fl_mlp_train(fl_mlp_t mlp, const float *X, const float *T, const float *M,
+                 int B, int epochs, float lr, float *losses);
+int fl_mlp_destroy(fl_mlp_t mlp);
+
 /* ---- allocation-free column sort -------------------------------------- */
 
 /* Largest column count fl_col_sort_noalloc accepts (its scratch array holds

@@ -1,0 +1,52 @@
+"""The CPU reference of the tuner network checks itself by finite
+differences (float64) -- so it can serve as the oracle of the CUDA
+gradients in tests/test_gpu_tuner.py."""
+import numpy as np
+
+from oracle import mlp
+
+
+def test_numpy_mlp_gradient_matches_finite_differences():
+    rng = np.random.default_rng(0)
+    shape = (5, 7, 6, 3)
+    n = 5 * 7 + 7 + 7 * 6 + 6 + 6 * 3 + 3
+    p = rng.normal(0, 0.5, n)
+    X = rng.normal(size=(11, 5))
+    T = rng.normal(size=(11, 3))
+    M = (rng.random((11, 3)) > 0.2).astype(float)
+    loss, g = mlp.loss_grad(p, shape, X, T, M)
+    eps = 1e-6
+    fd = np.empty(n)
+    for i in range(n):
+        q = p.copy()
+        q[i] += eps
+        lp, _ = mlp.loss_grad(q, shape, X, T, M)
+        q[i] -= 2 * eps
+        lm, _ = mlp.loss_grad(q, shape, X, T, M)
+        fd[i] = (lp - lm) / (2 * eps)
+    np.testing.assert_allclose(g, fd, rtol=1e-5, atol=1e-7)
+
+
+def test_tuner_targets_and_regret():
+    from fastload_gb300 import tuner
+
+    t = np.array([[2.0, 1.0, 4.0, 1.5, 3.0, 2.0], [1.0, 1.1, 1.2, 1.3, 1.4, 1.0]])
+    tg = tuner.targets(t)
+    np.testing.assert_allclose(tg[0], np.log2(t[0] / 1.0))
+    ev = tuner.evaluate(np.array([1, 0]), t)
+    assert ev["mean_regret"] == 0.0 and ev["frac_within_10pct"] == 1.0
+    assert ev["speedup_vs_auto_rule"] == (2.0 + 1.0) / (1.0 + 1.0)
+
+
+def test_tuner_specs_cover_the_families_and_ranges():
+    from fastload_gb300 import tuner
+
+    rng = np.random.default_rng(5)
+    specs = [tuner.sample_spec(rng, i) for i in range(200)]
+    assert {s["family"] for s in specs} == set(tuner.FAMILIES)
+    for s in specs[:40]:
+        assert tuner.N_RANGE[0] * 0.99 <= s["n"] <= tuner.N_RANGE[1] * 1.01
+        d = tuner.degrees(s)
+        assert d.shape == (s["n"],) and d.min() >= 0 and d.sum() <= tuner.NNZ_RANGE[1] * 1.06
+        if s["family"] == "banded":
+            assert d.max() <= max(1, int(s["param"]))
