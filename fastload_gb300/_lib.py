@@ -82,6 +82,8 @@ SIGNATURES = [
     ("fl_plan_spmv", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p]),
     ("fl_plan_spmv_host", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
     ("fl_plan_destroy", C.c_int, [C.c_void_p]),
+    ("fl_plan_save", C.c_int, [C.c_void_p, C.c_char_p]),
+    ("fl_plan_load", C.c_int, [C.POINTER(C.c_void_p), C.c_char_p, C.c_void_p]),
     ("fl_plan_add_form", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int)]),
     ("fl_plan_form_info", C.c_int, [C.c_void_p, C.c_int, C.POINTER(FormInfoC)]),
     ("fl_plan_spmv_form", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),

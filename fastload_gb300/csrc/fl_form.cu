@@ -49,6 +49,23 @@ __global__ void __launch_bounds__(256) k_untile(StepView st, int n, int tilenum,
     }
 }
 
+int untile_layout(const Layout &L, DevBuf<int> &srow, DevBuf<double> &sval, cudaStream_t s) {
+    const int n = L.n, nnz = L.nnz;
+    DevBuf<int> scolptr;
+    FL_TRY(scolptr.alloc((size_t)n + 1, s));
+    FL_TRY(scan_exclusive(L.sortnnz.get(), scolptr.get(), n, scolptr.get() + n, s));
+    FL_TRY(srow.alloc(std::max(nnz, 1), s));
+    FL_TRY(sval.alloc(std::max(nnz, 1), s));
+    if (L.tilenum > 0) {
+        const StepTable &st = L.st;
+        StepView sv{st.col.get(), st.base.get(), st.tall.get(), st.tile_off.get(), st.nnz_off.get(), st.steps};
+        k_untile<<<grid_n((long)L.tilenum * 32, 256, 16), 256, 0, s>>>(sv, n, L.tilenum, scolptr.get(), L.row.get(),
+                                                                       L.val.get(), srow.get(), sval.get());
+        FL_CUDA(cudaGetLastError());
+    }
+    return FL_SUCCESS;
+}
+
 __global__ void k_to_f32(const double *in, float *out, long n) {
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
         out[i] = (float)in[i];
@@ -82,19 +99,9 @@ int build_form(Form &F, const Layout &L, int vtype, int band, int yf32, cudaStre
     F.band = band;
     const int m = L.m, n = L.n, nnz = L.nnz;
     // the column-sorted CSC, recovered from the tile streams
-    DevBuf<int> scolptr, srow;
+    DevBuf<int> srow;
     DevBuf<double> sval;
-    FL_TRY(scolptr.alloc((size_t)n + 1, s));
-    FL_TRY(scan_exclusive(L.sortnnz.get(), scolptr.get(), n, scolptr.get() + n, s));
-    FL_TRY(srow.alloc(std::max(nnz, 1), s));
-    FL_TRY(sval.alloc(std::max(nnz, 1), s));
-    if (L.tilenum > 0) {
-        const StepTable &st = L.st;
-        StepView sv{st.col.get(), st.base.get(), st.tall.get(), st.tile_off.get(), st.nnz_off.get(), st.steps};
-        k_untile<<<grid_n((long)L.tilenum * 32, 256, 16), 256, 0, s>>>(sv, n, L.tilenum, scolptr.get(), L.row.get(),
-                                                                       L.val.get(), srow.get(), sval.get());
-        FL_CUDA(cudaGetLastError());
-    }
+    FL_TRY(untile_layout(L, srow, sval, s));
     int nh;
     bool wide = false;
     if (band == FL_BAND_NONE) {

@@ -245,6 +245,10 @@ int bucket_auto_band(const int *sortnnz, int n, int nnz, cudaStream_t s);
 
 int num_sms();
 
+// Column-sorted CSC (rows, values) of a layout, recovered from its tile
+// streams; needs L.sortnnz and the step table.
+int untile_layout(const Layout &L, DevBuf<int> &srow, DevBuf<double> &sval, cudaStream_t s);
+
 // Forms (fl_form.cu): build from a plan's FP64 layout, run.
 int build_form(Form &F, const Layout &L, int vtype, int band, int yf32, cudaStream_t s);
 int spmv_form(Form &F, int k, const void *xs, void *y, int accumulate, cudaStream_t s);

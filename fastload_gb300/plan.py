@@ -7,6 +7,7 @@ PyTorch tensors provide the device memory and the current stream.
 from __future__ import annotations
 
 import ctypes as C
+import struct
 
 import numpy as np
 
@@ -26,6 +27,65 @@ VALUES_BF16X2 = 2
 BAND_AUTO = 0
 BAND_NONE = -1
 BAND_ALL = -2
+
+
+PLAN_FILE_MAGIC = b"FLGBPLAN"
+_HEADER = struct.Struct("<8sIII9i5Q3QQ")  # 128 bytes, the layout of fl_cache.cu
+_HEADER_FIELDS = ("magic", "version", "header_bytes", "byte_order", "m", "n", "nnz", "tilenum", "steps",
+                  "with_ref", "heavy", "nforms", "reserved0")
+_SECTIONS = ("perm", "sortnnz", "row", "val", "forms")
+
+
+def plan_file_hash(data: bytes) -> int:
+    """Checksum of plan files: 64-bit FNV-1a over little-endian 64-bit words
+    (tail zero-padded), xor-ed with the byte count."""
+    h = 0xCBF29CE484222325
+    pad = (-len(data)) % 8
+    for (w,) in struct.iter_unpack("<Q", data + b"\0" * pad):
+        h = ((h ^ w) * 0x100000001B3) & 0xFFFFFFFFFFFFFFFF
+    return h ^ len(data)
+
+
+def plan_file_header(path) -> dict:
+    """Header of a plan file (fl_plan_save) as a dict; no GPU needed.  Raises
+    ValueError when the file is not a plan file or its header checksum fails."""
+    with open(path, "rb") as f:
+        raw = f.read(_HEADER.size)
+    if len(raw) != _HEADER.size or raw[:8] != PLAN_FILE_MAGIC:
+        raise ValueError(f"{path}: not a plan file")
+    v = _HEADER.unpack(raw)
+    d = dict(zip(_HEADER_FIELDS, v[:13]))
+    d["hashes"] = dict(zip(_SECTIONS, v[13:18]))
+    if plan_file_hash(raw[:120]) != v[21]:
+        raise ValueError(f"{path}: header checksum mismatch")
+    return d
+
+
+def plan_file_sections(path) -> dict:
+    """The arrays of a plan file (numpy views of its bytes)."""
+    h = plan_file_header(path)
+    n, nnz, nf = h["n"], h["nnz"], h["nforms"]
+    with open(path, "rb") as f:
+        f.seek(_HEADER.size)
+        out = {"perm": np.fromfile(f, "<i4", n), "sortnnz": np.fromfile(f, "<i4", n),
+               "row": np.fromfile(f, "<i4", nnz), "val": np.fromfile(f, "<f8", nnz),
+               "forms": np.fromfile(f, "<i4", 3 * nf).reshape(nf, 3)}
+    return out
+
+
+def write_plan_file(path, header: dict, sections: dict) -> None:
+    """Writes a plan file from a header dict and arrays, recomputing every
+    checksum (used to build test inputs)."""
+    body = [np.ascontiguousarray(sections[k], dt).tobytes()
+            for k, dt in zip(_SECTIONS, ("<i4", "<i4", "<i4", "<f8", "<i4"))]
+    hashes = [plan_file_hash(b) for b in body]
+    fields = [header[k] for k in _HEADER_FIELDS]
+    raw = _HEADER.pack(*fields, *hashes, 0, 0, 0, 0)[:120]
+    raw += struct.pack("<Q", plan_file_hash(raw))
+    with open(path, "wb") as f:
+        f.write(raw)
+        for b in body:
+            f.write(b)
 
 
 def _torch():
@@ -83,6 +143,18 @@ class Plan:
     def from_csc(cls, m: int, n: int, colptr, rowidx, val, with_reference_arrays: bool = False,
                  heavy_band: int = 0, stream=None):
         return cls.create(INPUT_CSC, m, n, colptr, rowidx, val, with_reference_arrays, heavy_band, stream)
+
+    @classmethod
+    def load(cls, path, stream=None):
+        """A plan read from a file written by save(): the same layout, heavy
+        band and forms, rebuilt on the current device."""
+        h = C.c_void_p()
+        check(load().fl_plan_load(C.byref(h), str(path).encode(), _stream_handle(stream)))
+        return cls(h)
+
+    def save(self, path) -> None:
+        """Writes the plan's preprocessed format, options and forms to path."""
+        check(load().fl_plan_save(self._h, str(path).encode()))
 
     # -- queries -------------------------------------------------------------
     def _info(self) -> dict:

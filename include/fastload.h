@@ -35,6 +35,7 @@ extern "C" {
 #define FL_ERR_OVERFLOW (-4)  /* a count does not fit the 32-bit index space */
 #define FL_ERR_INTERNAL (-5)  /* internal consistency check failed */
 #define FL_ERR_NOT_READY (-6) /* bounded device wait expired */
+#define FL_ERR_IO (-7)        /* file missing, unreadable, truncated or corrupt */
 
 /* Same members, order and types as the reference's slide_matrix
  * (src/format.h:6-20), so a pointer to either can be passed. */
@@ -196,6 +197,21 @@ int fl_plan_destroy(fl_plan_t plan);
 /* Reads and clears the device status word of the plan's kernels (0 when no
  * bounded wait expired); synchronises the device. */
 int fl_plan_check(fl_plan_t plan);
+
+/* ---- persistent plan files ------------------------------------------- */
+
+/* Writes the plan's preprocessed FastLoad format to `path`: the column
+ * permutation, nonzeros per sorted column, the tile-ordered row and value
+ * streams (the reference's sortrowidx / sortval), the plan options and the
+ * list of forms, with checksums.  Replaces rebuilding (and re-uploading,
+ * src/FastLoad_GPU.h:318-327) the format on every run of the reference's
+ * src/main.cu:314.  Synchronises the device. */
+int fl_plan_save(fl_plan_t plan, const char *path);
+/* Reads a plan file into a new device plan equal to the saved one (same
+ * layout, heavy band and forms).  FL_ERR_IO for a missing, truncated or
+ * corrupt file (checksums), FL_ERR_ARG when the content is not a valid
+ * FastLoad format (permutation, ascending column counts, row range). */
+int fl_plan_load(fl_plan_t *plan, const char *path, void *stream);
 
 /* ---- storage / right-hand-side forms ---------------------------------- */
 
