@@ -52,6 +52,12 @@ class PlanOptsC(C.Structure):
     _fields_ = [("with_reference_arrays", C.c_int), ("heavy_band", C.c_int), ("reserved", C.c_int * 6)]
 
 
+class MtxInfoC(C.Structure):
+    _fields_ = [("m", C.c_int), ("n", C.c_int), ("nnz", C.c_int), ("nnz_file", C.c_int), ("field", C.c_int),
+                ("symmetry", C.c_int), ("is_symmetric", C.c_int), ("exact_path_values", C.c_int),
+                ("file_bytes", C.c_size_t)]
+
+
 # (name, restype, argtypes) of every exported symbol; tests check the .so
 # exports each one and that include/fastload.h declares each one.
 SIGNATURES = [
@@ -82,6 +88,14 @@ SIGNATURES = [
     ("fl_plan_spmv", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p]),
     ("fl_plan_spmv_host", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
     ("fl_plan_destroy", C.c_int, [C.c_void_p]),
+    ("fl_mtx_read", C.c_int, [C.POINTER(C.c_void_p), C.c_char_p, C.c_void_p]),
+    ("fl_mtx_info_get", C.c_int, [C.c_void_p, C.POINTER(MtxInfoC)]),
+    ("fl_mtx_csr", C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]),
+    ("fl_mtx_copy_csr", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("fl_mtx_destroy", C.c_int, [C.c_void_p]),
+    ("fl_mmio_allinone", C.c_int, [C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                   C.POINTER(C.POINTER(C.c_int)), C.POINTER(C.POINTER(C.c_int)),
+                                   C.POINTER(C.POINTER(C.c_double)), C.c_char_p]),
     ("fl_plan_save", C.c_int, [C.c_void_p, C.c_char_p]),
     ("fl_plan_load", C.c_int, [C.POINTER(C.c_void_p), C.c_char_p, C.c_void_p]),
     ("fl_plan_add_form", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int)]),

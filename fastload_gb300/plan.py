@@ -145,6 +145,20 @@ class Plan:
         return cls.create(INPUT_CSC, m, n, colptr, rowidx, val, with_reference_arrays, heavy_band, stream)
 
     @classmethod
+    def from_mtx(cls, path, with_reference_arrays: bool = False, heavy_band: int = 0, stream=None):
+        """A plan of a MatrixMarket file, parsed on the GPU (mtx.Mtx) and
+        handed over as device CSR without a host round trip."""
+        from .mtx import Mtx
+
+        with Mtx.read(path, stream) as mt:
+            rp, ci, v = mt.device_pointers()
+            o = PlanOptsC(int(with_reference_arrays), int(heavy_band))
+            h = C.c_void_p()
+            check(load().fl_plan_create(C.byref(h), INPUT_CSR, mt.m, mt.n, mt.nnz, C.c_void_p(rp), C.c_void_p(ci),
+                                        C.c_void_p(v), C.byref(o), _stream_handle(stream)))
+        return cls(h)
+
+    @classmethod
     def load(cls, path, stream=None):
         """A plan read from a file written by save(): the same layout, heavy
         band and forms, rebuilt on the current device."""

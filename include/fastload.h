@@ -213,6 +213,58 @@ int fl_plan_save(fl_plan_t plan, const char *path);
  * FastLoad format (permutation, ascending column counts, row range). */
 int fl_plan_load(fl_plan_t *plan, const char *path, void *stream);
 
+/* ---- MatrixMarket ingest on the GPU ------------------------------------ */
+
+/* Data type and storage scheme of a .mtx file (banner fields 4 and 5). */
+#define FL_MTX_REAL 0
+#define FL_MTX_INTEGER 1
+#define FL_MTX_PATTERN 2
+#define FL_MTX_COMPLEX 3
+#define FL_MTX_GENERAL 0
+#define FL_MTX_SYMMETRIC 1
+#define FL_MTX_HERMITIAN 2
+#define FL_MTX_SKEW 3
+
+typedef struct fl_mtx *fl_mtx_t;
+
+typedef struct fl_mtx_info {
+    int m, n;
+    int nnz;          /* CSR nonzeros after symmetric expansion (mmio_allinone's *nnz) */
+    int nnz_file;     /* entries stored in the file */
+    int field;        /* FL_MTX_REAL / INTEGER / PATTERN / COMPLEX */
+    int symmetry;     /* FL_MTX_GENERAL / SYMMETRIC / HERMITIAN / SKEW */
+    int is_symmetric; /* mmio_allinone's *isSymmetric: symmetric or hermitian */
+    int exact_path_values; /* values decided by the big-integer comparison */
+    size_t file_bytes;
+} fl_mtx_info;
+
+/* Reads a coordinate .mtx file into device CSR: the banner and size line on
+ * the host, the entries tokenised, converted and assembled on the GPU.
+ * Produces exactly the CSR of the reference's mmio_allinone
+ * (src/auxiliary.h:64-232): rows in file order, symmetric / hermitian
+ * entries mirrored, values correctly rounded as strtod rounds them.
+ * Synchronous on `stream`.  FL_ERR_IO for unreadable files, FL_ERR_ARG for
+ * malformed or unsupported content (array files, indices out of range, too
+ * few entries, hexadecimal floats, NaN payloads). */
+int fl_mtx_read(fl_mtx_t *mtx, const char *path, void *stream);
+int fl_mtx_info_get(fl_mtx_t mtx, fl_mtx_info *info);
+/* Device CSR of the file (row pointer m+1, column indices and values nnz),
+ * owned by the handle and valid until fl_mtx_destroy.  Any output may be
+ * NULL. */
+int fl_mtx_csr(fl_mtx_t mtx, const int **d_rowptr, const int **d_colidx,
+               const double **d_val);
+/* Copies the CSR into caller device buffers (m+1, nnz, nnz entries; any
+ * may be NULL), asynchronously on `stream`. */
+int fl_mtx_copy_csr(fl_mtx_t mtx, int *d_rowptr, int *d_colidx, double *d_val,
+                    void *stream);
+int fl_mtx_destroy(fl_mtx_t mtx);
+/* Replaces mmio_allinone (src/auxiliary.h:64-232) with the same outputs:
+ * host arrays from malloc (freed by the caller), parsed on the GPU.
+ * Returns 0 or a negative FL_ERR_* status. */
+int fl_mmio_allinone(int *m, int *n, int *nnz, int *isSymmetric,
+                     int **csrrowptr, int **csrcolidx, double **csrval,
+                     const char *filename);
+
 /* ---- storage / right-hand-side forms ---------------------------------- */
 
 /* Value storage of a form. */

@@ -44,6 +44,7 @@ def lib() -> C.CDLL:
             "fo_csc_spmv": (None, [I, _P, _P, _P, _P, _P]),
             "fo_csr_spmv": (None, [I, _P, _P, _P, _P, _P]),
             "fo_csc_spmv_dd": (None, [I, I, I, _P, _P, _P, _P, _P]),
+            "fo_mmio_read": (I, [C.c_char_p, C.POINTER(I), C.POINTER(I), C.POINTER(I), C.POINTER(I), _P, _P, _P]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -164,6 +165,21 @@ def csc_spmv_dd(m, n, cscptr, cscrow, cscval, x, k: int = 1):
     y = np.zeros(m * k)
     lib().fo_csc_spmv_dd(m, n, k, _p(_i(cscptr)), _p(_i(cscrow)), _p(_d(cscval)), _p(_d(x)), _p(y))
     return y if k == 1 else y.reshape(m, k)
+
+
+def mmio_read(path):
+    """(m, n, nnz, is_symmetric, rowptr, colidx, val) of a coordinate .mtx
+    file, read as the reference's mmio_allinone reads it."""
+    m, n, nnz, sym = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+    L = lib()
+    rc = L.fo_mmio_read(str(path).encode(), C.byref(m), C.byref(n), C.byref(nnz), C.byref(sym), None, None, None)
+    if rc:
+        raise ValueError(f"fo_mmio_read failed ({rc}) for {path}")
+    rp, ci, v = np.empty(m.value + 1, np.int32), np.empty(max(nnz.value, 1), np.int32), np.empty(max(nnz.value, 1))
+    rc = L.fo_mmio_read(str(path).encode(), C.byref(m), C.byref(n), C.byref(nnz), C.byref(sym), _p(rp), _p(ci), _p(v))
+    if rc:
+        raise ValueError(f"fo_mmio_read failed ({rc}) for {path}")
+    return m.value, n.value, nnz.value, sym.value, rp, ci[:nnz.value], v[:nnz.value]
 
 
 def rel_errors(y, yref):

@@ -8,7 +8,9 @@
  */
 #include "fl_oracle.h"
 
+#include <ctype.h>
 #include <math.h>
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 #ifdef _OPENMP
@@ -303,4 +305,116 @@ void fo_csc_spmv_dd(int m, int n, int k, const int *cscptr,
     }
     for (size_t i = 0; i < cnt; i++) y[i] += lo[i];
     free(lo);
+}
+
+/* ------------------------------------------------------- MatrixMarket -- */
+/* Banner: five fields, the first starting with %%MatrixMarket, the others
+ * compared in lower case (src/mmio.h:172-259).  field: 'R','I','P','C';
+ * storage: 'G','S','H','K'. */
+static int mm_banner(FILE *f, char *field, char *storage)
+{
+    char line[1025], b[1025], obj[1025], fmt[1025], typ[1025], sto[1025];
+    if (!fgets(line, sizeof line, f)) return -2;
+    if (sscanf(line, "%s %s %s %s %s", b, obj, fmt, typ, sto) != 5) return -2;
+    for (char *p = obj; *p; p++) *p = (char)tolower((unsigned char)*p);
+    for (char *p = fmt; *p; p++) *p = (char)tolower((unsigned char)*p);
+    for (char *p = typ; *p; p++) *p = (char)tolower((unsigned char)*p);
+    for (char *p = sto; *p; p++) *p = (char)tolower((unsigned char)*p);
+    if (strncmp(b, "%%MatrixMarket", 14) != 0) return -2;
+    if (strcmp(obj, "matrix") != 0 || strcmp(fmt, "coordinate") != 0) return -2;
+    if (!strcmp(typ, "real")) *field = 'R';
+    else if (!strcmp(typ, "integer")) *field = 'I';
+    else if (!strcmp(typ, "pattern")) *field = 'P';
+    else if (!strcmp(typ, "complex")) *field = 'C';
+    else return -2;
+    if (!strcmp(sto, "general")) *storage = 'G';
+    else if (!strcmp(sto, "symmetric")) *storage = 'S';
+    else if (!strcmp(sto, "hermitian")) *storage = 'H';
+    else if (!strcmp(sto, "skew-symmetric")) *storage = 'K';
+    else return -2;
+    return 0;
+}
+
+/* Size line after the comment lines (src/mmio.h:142-170). */
+static int mm_size(FILE *f, int *m, int *n, int *nz)
+{
+    char line[1025];
+    do {
+        if (!fgets(line, sizeof line, f)) return -4;
+    } while (line[0] == '%');
+    if (sscanf(line, "%d %d %d", m, n, nz) == 3) return 0;
+    /* a blank line: the sizes are the next three tokens (a token that is not
+     * an integer is an error; the reference would spin on it) */
+    return fscanf(f, "%d %d %d", m, n, nz) == 3 ? 0 : -4;
+}
+
+int fo_mmio_read(const char *path, int *m, int *n, int *nnz, int *is_symmetric,
+                 int *rowptr, int *colidx, double *val)
+{
+    FILE *f = fopen(path, "r");
+    if (!f) return -1;
+    char field = 0, storage = 0;
+    int rc = mm_banner(f, &field, &storage);
+    int M = 0, N = 0, NZ = 0;
+    if (!rc) rc = mm_size(f, &M, &N, &NZ);
+    if (rc) {
+        fclose(f);
+        return rc;
+    }
+    const int sym = storage == 'S' || storage == 'H';
+    if (sym && M != N) { /* mirrored entries would fall outside the matrix */
+        fclose(f);
+        return -5;
+    }
+    int *ri = (int *)malloc(sizeof(int) * (NZ ? NZ : 1));
+    int *ci = (int *)malloc(sizeof(int) * (NZ ? NZ : 1));
+    double *vv = (double *)malloc(sizeof(double) * (NZ ? NZ : 1));
+    int *cnt = (int *)calloc((size_t)M + 1, sizeof(int));
+    rc = (ri && ci && vv && cnt) ? 0 : -5;
+    for (int i = 0; i < NZ && !rc; i++) {
+        int r, c, iv, got;
+        double v = 1.0, im;
+        if (field == 'R') got = fscanf(f, "%d %d %lg", &r, &c, &v) == 3;
+        else if (field == 'C') got = fscanf(f, "%d %d %lg %lg", &r, &c, &v, &im) == 4;
+        else if (field == 'I') {
+            got = fscanf(f, "%d %d %d", &r, &c, &iv) == 3;
+            v = iv;
+        } else got = fscanf(f, "%d %d", &r, &c) == 2;
+        if (!got || r < 1 || r > M || c < 1 || c > N) {
+            rc = -5;
+            break;
+        }
+        ri[i] = r - 1;
+        ci[i] = c - 1;
+        vv[i] = v;
+        cnt[r - 1]++;
+        if (sym && r != c) cnt[c - 1]++;
+    }
+    fclose(f);
+    if (!rc) {
+        excl_scan(cnt, (long)M + 1);
+        *m = M;
+        *n = N;
+        *nnz = cnt[M];
+        *is_symmetric = sym;
+        if (rowptr) {
+            memcpy(rowptr, cnt, sizeof(int) * ((size_t)M + 1));
+            /* fill rows in file order; a mirrored entry follows its original */
+            for (int i = 0; i < NZ; i++) {
+                int p = cnt[ri[i]]++;
+                colidx[p] = ci[i];
+                val[p] = vv[i];
+                if (sym && ri[i] != ci[i]) {
+                    p = cnt[ci[i]]++;
+                    colidx[p] = ri[i];
+                    val[p] = vv[i];
+                }
+            }
+        }
+    }
+    free(ri);
+    free(ci);
+    free(vv);
+    free(cnt);
+    return rc;
 }

@@ -94,6 +94,19 @@ void fo_csc_spmv_dd(int m, int n, int k, const int *cscptr,
                     const int *cscrow, const double *cscval, const double *x,
                     double *y);
 
+/* MatrixMarket coordinate file -> CSR, restating mmio_allinone
+ * (src/auxiliary.h:64-232) with the banner / size-line rules of
+ * src/mmio.h:142-259: entries read by fscanf in file order ("%d %d %lg",
+ * "%d %d %d", "%d %d", or two values for complex keeping the real part),
+ * symmetric and hermitian entries mirrored, rows filled in file order.
+ * Call with rowptr == NULL for the sizes (m, n, expanded nnz, symmetric
+ * flag), then again with arrays of m+1 / nnz / nnz entries.  Returns 0, -1
+ * (cannot open), -2 (banner), -4 (size line), -5 (an entry that does not
+ * scan or lies outside the matrix: the reference would read garbage or
+ * write out of bounds there). */
+int fo_mmio_read(const char *path, int *m, int *n, int *nnz, int *is_symmetric,
+                 int *rowptr, int *colidx, double *val);
+
 #ifdef __cplusplus
 }
 #endif
