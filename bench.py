@@ -323,6 +323,56 @@ def measure_batch(fl, peak, reps=10):
     return out
 
 
+def measure_comparators(fl, c, x, ydd, B, reps=20):
+    """The reference's comparators on the bench matrix, timed like the
+    FastLoad kernel (CUDA events per launch, y zeroing outside): its naive
+    CSC kernel and cuSPARSE CSR SpMV (each algorithm, handle prepared once).
+    GB/s use the same algorithmic bytes as the FastLoad line."""
+    import scipy.sparse as sp
+    import torch
+
+    import oracle
+    from fastload_gb300 import compare
+
+    stream = torch.cuda.current_stream()
+    dev = lambda a, t: torch.from_numpy(np.ascontiguousarray(a)).to("cuda", t)  # noqa: E731
+    cp, cr, cv = dev(c.colptr, torch.int32), dev(c.rowidx, torch.int32), dev(c.val, torch.float64)
+    y = torch.zeros(c.m, dtype=torch.float64, device="cuda")
+    out = {}
+
+    def timed(fn, n_reps):
+        for _ in range(3):
+            fn()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ts = []
+        for _ in range(n_reps):
+            y.zero_()
+            a.record(stream)
+            fn()
+            b.record(stream)
+            b.synchronize()
+            ts.append(a.elapsed_time(b))
+        return float(np.mean(ts))
+
+    def entry(ms):
+        err = oracle.rel_errors(y.cpu().numpy(), ydd)
+        return {"ms": ms, "gbs": B / (ms * 1e-3) / 1e9, "gflops": 2.0 * c.nnz / (ms * 1e-3) / 1e9,
+                "rel_err_normwise": err[0]}
+
+    ms = timed(lambda: compare.csc_spmv_naive(c.m, cp, cr, cv, x, y=y, accumulate=True), reps)
+    out["naive_csc"] = entry(ms)
+    del cp, cr, cv
+    A = sp.csc_matrix((c.val, c.rowidx, c.colptr), shape=(c.m, c.n)).tocsr()
+    rp, ci, v = dev(A.indptr, torch.int32), dev(A.indices, torch.int32), dev(A.data, torch.float64)
+    for alg, name in ((0, "cusparse_csr_default"), (1, "cusparse_csr_alg1"), (2, "cusparse_csr_alg2")):
+        try:
+            with compare.CuSparse(c.m, c.n, rp, ci, v, alg=alg) as cs:
+                out[name] = entry(timed(lambda: cs.spmv(x, y=y), reps))
+        except fl.FastLoadError as e:
+            out[name] = {"unavailable": str(e)}
+    return out
+
+
 def run_profile(spec):
     """--profile case:values:band:k -- builds one case and runs one kernel a
     few times (for ncu captures).  case lap128 | zipf | zipf<n>; values
@@ -459,6 +509,8 @@ def run_gpu(args, rank, world):
     e2e_rel = oracle.rel_errors(hy, ydd)
 
     peak, peak_kind = measured_peaks()
+    comparators = (measure_comparators(fl, c, x, ydd, B) if (rank == 0 and not args.quick and not args.no_compare)
+                   else None)
     forms = measure_forms(fl, peak) if (rank == 0 and not args.quick and not args.no_forms) else None
     batch = measure_batch(fl, peak) if (rank == 0 and not args.quick and not args.no_forms) else None
     if rank != 0:
@@ -485,6 +537,7 @@ def run_gpu(args, rank, world):
         "kernel_variants_gbs": variants,
         "speedup_vs_plain_fp64_stream": (variants["stream2"] and achieved / variants["stream2"]) if variants else None,
         "preprocess_s": prep_s,
+        "comparators": comparators,
         "forms": forms,
         "batch": batch,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -512,6 +565,7 @@ def main():
     ap.add_argument("--n", type=int, default=N_COLS, help="columns of the Zipf matrix (default 1,048,576)")
     ap.add_argument("--profile", default=None, help="case:values:band:k -- run one kernel for a profiler")
     ap.add_argument("--no-forms", action="store_true", help="skip the storage / multi-RHS form measurements")
+    ap.add_argument("--no-compare", action="store_true", help="skip the naive-CSC and cuSPARSE comparator lines")
     ap.add_argument("--quick", action="store_true", help="skip kernel variants, shorten e2e and CPU legs "
                                                          "(for profiling runs)")
     args = ap.parse_args()

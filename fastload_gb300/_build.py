@@ -76,7 +76,7 @@ def build_library(force: bool = False, verbose: bool = False) -> str:
     with cf.ThreadPoolExecutor(max_workers=min(len(srcs), os.cpu_count() or 4)) as ex:
         objs = list(ex.map(_compile, srcs))
     tmp = target + ".tmp"
-    cmd = [nvcc(), *ARCH, "-shared", "-cudart", "shared", "-o", tmp, *objs]
+    cmd = [nvcc(), *ARCH, "-shared", "-cudart", "shared", "-o", tmp, *objs, "-ldl"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

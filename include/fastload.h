@@ -36,6 +36,7 @@ extern "C" {
 #define FL_ERR_INTERNAL (-5)  /* internal consistency check failed */
 #define FL_ERR_NOT_READY (-6) /* bounded device wait expired */
 #define FL_ERR_IO (-7)        /* file missing, unreadable, truncated or corrupt */
+#define FL_ERR_UNAVAILABLE (-8) /* optional component missing (cuSPARSE comparator) */
 
 /* Same members, order and types as the reference's slide_matrix
  * (src/format.h:6-20), so a pointer to either can be passed. */
@@ -264,6 +265,31 @@ int fl_mtx_destroy(fl_mtx_t mtx);
 int fl_mmio_allinone(int *m, int *n, int *nnz, int *isSymmetric,
                      int **csrrowptr, int **csrcolidx, double **csrval,
                      const char *filename);
+
+/* ---- comparators (context lines for reports, never a fallback) --------- */
+
+/* y = A x (y zeroed first unless accumulate) with the reference's naive CSC
+ * kernel: one thread per column, one atomic per nonzero, 32 blocks of 64
+ * threads per SM (src/CSCSpMV.h:4-27, launch at :68).  Device CSC in
+ * original column order, x in original order.  Asynchronous on `stream`. */
+int fl_csc_spmv_naive(int m, int n, int nnz, const int *d_colptr,
+                      const int *d_rowidx, const double *d_val,
+                      const double *d_x, double *d_y, int accumulate,
+                      void *stream);
+
+typedef struct fl_cusparse *fl_cusparse_t;
+/* cuSPARSE CSR FP64 SpMV, the reference's second comparator
+ * (src/cusparse_cuda.h:27-155), prepared once (buffer + preprocess) so that
+ * fl_cusparse_spmv times the steady state.  alg: 0 CUSPARSE_SPMV_ALG_DEFAULT,
+ * 1 CSR_ALG1, 2 CSR_ALG2.  The device CSR must outlive the handle.
+ * libcusparse is loaded on first use; FL_ERR_UNAVAILABLE without it. */
+int fl_cusparse_create(fl_cusparse_t *h, int m, int n, int nnz,
+                       const int *d_rowptr, const int *d_colidx,
+                       const double *d_val, int alg, void *stream);
+/* y = A x, asynchronous on `stream`. */
+int fl_cusparse_spmv(fl_cusparse_t h, const double *d_x, double *d_y,
+                     void *stream);
+int fl_cusparse_destroy(fl_cusparse_t h);
 
 /* ---- storage / right-hand-side forms ---------------------------------- */
 
