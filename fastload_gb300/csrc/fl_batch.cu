@@ -34,7 +34,7 @@ struct fl_batch {
     DevBuf<ItemDesc> items;
     int nitems = 0;
     DevBuf<int> perm;  // stacked sorted position -> stacked original column
-    DevBuf<int> err, next;
+    DevBuf<int> err;
     // captured graph and the pointers it was captured with
     cudaGraphExec_t exec = nullptr;
     const void *g_xs = nullptr;
@@ -93,7 +93,6 @@ int launch(fl_batch *b, const void *xs, void *y, cudaStream_t s) {
     const size_t ysz = b->yf32 ? sizeof(float) : sizeof(double);
     if (b->M) FL_CUDA(cudaMemsetAsync(y, 0, (size_t)b->M * ysz, s));
     if (b->nitems == 0) return FL_SUCCESS;
-    FL_CUDA(cudaMemsetAsync(b->next.get(), 0, sizeof(int), s));
     auto fill = [&](auto &a) {
         a.items = b->items.get();
         a.regions = b->regions.get();
@@ -110,7 +109,6 @@ int launch(fl_batch *b, const void *xs, void *y, cudaStream_t s) {
         a.hcol16 = nullptr;
         a.hcol32 = nullptr;
         a.err = b->err.get();
-        a.next = b->next.get();
     };
     if (b->vtype == FL_VALUES_F64) {
         FormArgs<double, double> a;
@@ -229,7 +227,6 @@ int fl_batch_create(fl_batch_t *out, int count, const fl_plan_t *plans, int valu
     FL_CUDA(cudaMemcpyAsync(b->items.get(), itm.data(), itm.size() * sizeof(ItemDesc), cudaMemcpyHostToDevice, s));
     FL_CUDA(cudaMemcpyAsync(b->perm.get(), perm.data(), perm.size() * sizeof(int), cudaMemcpyHostToDevice, s));
     FL_TRY(b->err.alloc(1, s));
-    FL_TRY(b->next.alloc(1, s));
     FL_CUDA(cudaMemsetAsync(b->err.get(), 0, sizeof(int), s));
     FL_CUDA(cudaStreamSynchronize(s));
     *out = b.release();

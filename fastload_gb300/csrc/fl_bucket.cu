@@ -131,7 +131,6 @@ int build_bucket(Bucket &B, int m, int n, int nnz, const int *sortnnz, const int
     H.nnz = (long)nnz - nnz_l;
     FL_TRY(B.err.alloc(1, s));
     FL_CUDA(cudaMemsetAsync(B.err.get(), 0, sizeof(int), s));
-    FL_TRY(B.next.alloc(1, s));
     if (nh == 0 || H.nnz == 0) {
         H.nh = 0;
         return FL_SUCCESS;
@@ -239,12 +238,10 @@ int spmv_bucket_f64(const Bucket &B, const double *xs, double *y, cudaStream_t s
     a.xs = xs;
     a.y = y;
     a.err = B.err.get();
-    a.next = B.next.get();
     a.heavy_mode = 0;
     const size_t bytes = (size_t)a.nh * sizeof(double);
     a.bulk = a.nh > 0 && ((uintptr_t)(xs + H.H0) % 16 == 0) && bytes % 16 == 0;
     if (a.nitems == 0 && a.nunits == 0) return FL_SUCCESS;
-    FL_CUDA(cudaMemsetAsync(a.next, 0, sizeof(int), s));
     return run_form_f64(a, 1, H.nh > 65535, s);
 }
 

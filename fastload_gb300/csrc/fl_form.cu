@@ -155,7 +155,6 @@ static FormArgs<V, Y> form_args(Form &F, const V *lval, const V *hval, const voi
     a.xs = (const typename VT<V>::X *)xs;
     a.y = (Y *)y;
     a.err = B.err.get();
-    a.next = B.next.get();
     a.heavy_mode = 0;
     a.bulk = 0;
     return a;
@@ -176,7 +175,6 @@ int spmv_form(Form &F, int k, const void *xs, void *y, int accumulate, cudaStrea
     const int mode = light ? 0 : (!accumulate && B.heavy.nrows == m ? 2 : 1);
     if (!accumulate && m && mode != 2) FL_CUDA(cudaMemsetAsync(y, 0, (size_t)m * k * ysz, s));
     if (!light && B.heavy.nnz == 0) return FL_SUCCESS;
-    FL_CUDA(cudaMemsetAsync(B.next.get(), 0, sizeof(int), s));
     const HeavyBand &H = B.heavy;
     const size_t band_bytes = (size_t)H.nh * k * xsz;
     const bool bulk = H.nh > 0 && ((uintptr_t)((const char *)xs + (size_t)H.H0 * k * xsz) % 16 == 0) &&

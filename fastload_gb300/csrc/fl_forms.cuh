@@ -46,7 +46,6 @@ struct FormArgs {
     const X *xs;
     Y *y;
     int *err;
-    int *next;
 };
 
 // K > 1 light item: K lanes per nonzero, lane (g, r) adds the rhs-r product
@@ -201,8 +200,10 @@ __global__ void __launch_bounds__(FM_THREADS, 1) k_spmv_form(const FormArgs<V, Y
     extern __shared__ __align__(128) unsigned char fm_smem[];
     X *xh = (X *)fm_smem;
     __shared__ __align__(8) unsigned long long mbar;
+    __shared__ int claimed;  // units of this block handed out so far
     const int tid = threadIdx.x, lane = tid & 31;
     const uint32_t bar = (uint32_t)__cvta_generic_to_shared(&mbar);
+    if (tid == 0) claimed = 0;
     const bool use_band = a.nh > 0 && a.nslices > 0;
     if (XS && use_band) {
         const uint32_t bytes = (uint32_t)a.nh * K * (uint32_t)sizeof(X);
@@ -235,11 +236,19 @@ __global__ void __launch_bounds__(FM_THREADS, 1) k_spmv_form(const FormArgs<V, Y
     const X *xsrc = XS ? (const X *)xh : a.xs + (size_t)a.H0 * K;
     const int total = a.nitems + (use_band ? a.nunits : 0);
     bool staged = !(XS && use_band && a.bulk);
+    // Work distribution: unit u (light items first, then heavy units) goes
+    // to block u % gridDim.x, so every block gets an even share of both
+    // kinds; inside the block warps claim the block's units through a
+    // shared-memory counter.  No global atomics, no per-launch reset.
+    __syncthreads();
+    const int G = gridDim.x;
+    const int mine = total > (int)blockIdx.x ? (total - 1 - (int)blockIdx.x) / G + 1 : 0;
     for (;;) {
-        int u = 0;
-        if (lane == 0) u = atomicAdd(a.next, 1);
-        u = __shfl_sync(FULLM, u, 0);
-        if (u >= total) break;
+        int k = 0;
+        if (lane == 0) k = atomicAdd(&claimed, 1);
+        k = __shfl_sync(FULLM, k, 0);
+        if (k >= mine) break;
+        const int u = (int)blockIdx.x + G * k;
         if (u < a.nitems) {
             if constexpr (K == 1) stream_item<V, Y, 1>(a.items[u], a.regions, a.row, a.val, a.xs, a.y, lane);
             else light_item_kn<V, K, Y>(a.items[u], a.regions, a.row, a.val, a.xs, a.y, lane);

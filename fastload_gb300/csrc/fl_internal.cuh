@@ -149,7 +149,6 @@ struct Bucket {
     Layout light;
     HeavyBand heavy;
     DevBuf<int> err;            // device status word of the bucket kernel
-    DevBuf<int> next;           // work counter of the bucket kernel (zeroed per launch)
 };
 
 // A storage / right-hand-side form of a plan: its own bucketed split (light
