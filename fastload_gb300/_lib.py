@@ -102,6 +102,10 @@ SIGNATURES = [
                                      C.c_void_p, C.c_int, C.c_void_p]),
     ("fl_cusparse_spmv", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("fl_cusparse_destroy", C.c_int, [C.c_void_p]),
+    ("fl_csc_spmv_naive_host", C.c_int, [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                         C.c_void_p, C.c_int, C.POINTER(C.c_double)]),
+    ("fl_cusparse_spmv_host", C.c_int, [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                        C.c_void_p, C.c_int, C.POINTER(C.c_double)]),
     ("fl_plan_save", C.c_int, [C.c_void_p, C.c_char_p]),
     ("fl_plan_load", C.c_int, [C.POINTER(C.c_void_p), C.c_char_p, C.c_void_p]),
     ("fl_plan_add_form", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int)]),

@@ -172,3 +172,77 @@ extern "C" int fl_cusparse_destroy(fl_cusparse_t h) {
     delete h;
     return FL_SUCCESS;
 }
+
+namespace {
+
+// Host-buffer helper: uploads, runs `launch` reps times between events, y back.
+template <typename F>
+int host_timed(int m, int n, int nnz, const int *ptr, int nptr, const int *idx, const double *val, const double *x,
+               double *y, int reps, double *mean_ms, F launch) {
+    if (m < 0 || n < 0 || nnz < 0 || reps < 1 || !ptr || !x || !y || !mean_ms || (nnz && (!idx || !val)))
+        return fail(FL_ERR_ARG, "comparator: bad arguments (m=%d n=%d nnz=%d reps=%d)", m, n, nnz, reps);
+    const cudaStream_t s = 0;
+    DevBuf<int> dp, di;
+    DevBuf<double> dv, dx, dy;
+    FL_TRY(dp.alloc(nptr, s));
+    FL_TRY(di.alloc(std::max(nnz, 1), s));
+    FL_TRY(dv.alloc(std::max(nnz, 1), s));
+    FL_TRY(dx.alloc(std::max(n, 1), s));
+    FL_TRY(dy.alloc(std::max(m, 1), s));
+    FL_CUDA(cudaMemcpyAsync(dp.get(), ptr, (size_t)nptr * sizeof(int), cudaMemcpyHostToDevice, s));
+    if (nnz) {
+        FL_CUDA(cudaMemcpyAsync(di.get(), idx, (size_t)nnz * sizeof(int), cudaMemcpyHostToDevice, s));
+        FL_CUDA(cudaMemcpyAsync(dv.get(), val, (size_t)nnz * sizeof(double), cudaMemcpyHostToDevice, s));
+    }
+    if (n) FL_CUDA(cudaMemcpyAsync(dx.get(), x, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, s));
+    cudaEvent_t a, b;
+    FL_CUDA(cudaEventCreate(&a));
+    FL_CUDA(cudaEventCreate(&b));
+    struct Ev {
+        cudaEvent_t a, b;
+        ~Ev() { cudaEventDestroy(a); cudaEventDestroy(b); }
+    } ev{a, b};
+    FL_TRY(launch(dp.get(), di.get(), dv.get(), dx.get(), dy.get()));  // untimed: first-call set-up
+    double total = 0;
+    for (int r = 0; r < reps; r++) {
+        if (m) FL_CUDA(cudaMemsetAsync(dy.get(), 0, (size_t)m * sizeof(double), s));
+        FL_CUDA(cudaEventRecord(a, s));
+        FL_TRY(launch(dp.get(), di.get(), dv.get(), dx.get(), dy.get()));
+        FL_CUDA(cudaEventRecord(b, s));
+        FL_CUDA(cudaEventSynchronize(b));
+        float t = 0;
+        FL_CUDA(cudaEventElapsedTime(&t, a, b));
+        total += t;
+    }
+    if (m) FL_CUDA(cudaMemcpy(y, dy.get(), (size_t)m * sizeof(double), cudaMemcpyDeviceToHost));
+    *mean_ms = total / reps;
+    return FL_SUCCESS;
+}
+
+}  // namespace
+
+extern "C" int fl_csc_spmv_naive_host(int m, int n, int nnz, const int *csc_ptr, const int *csc_rowidx,
+                                      const double *csc_val, const double *x, double *y, int reps,
+                                      double *mean_ms) {
+    clear_error();
+    return host_timed(m, n, nnz, csc_ptr, n + 1, csc_rowidx, csc_val, x, y, reps, mean_ms,
+                      [&](const int *p, const int *i, const double *v, const double *dx, double *dy) {
+                          return fl_csc_spmv_naive(m, n, nnz, p, i, v, dx, dy, 1, nullptr);
+                      });
+}
+
+extern "C" int fl_cusparse_spmv_host(int m, int n, int nnz, const int *csr_rowptr, const int *csr_colidx,
+                                     const double *csr_val, const double *x, double *y, int reps,
+                                     double *mean_ms) {
+    clear_error();
+    fl_cusparse_t h = nullptr;
+    std::unique_ptr<fl_cusparse> guard;
+    return host_timed(m, n, nnz, csr_rowptr, m + 1, csr_colidx, csr_val, x, y, reps, mean_ms,
+                      [&](const int *p, const int *i, const double *v, const double *dx, double *dy) {
+                          if (!h) {
+                              FL_TRY(fl_cusparse_create(&h, m, n, nnz, p, i, v, 0, nullptr));
+                              guard.reset(h);
+                          }
+                          return fl_cusparse_spmv(h, dx, dy, nullptr);
+                      });
+}

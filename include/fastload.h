@@ -290,6 +290,18 @@ int fl_cusparse_create(fl_cusparse_t *h, int m, int n, int nnz,
 int fl_cusparse_spmv(fl_cusparse_t h, const double *d_x, double *d_y,
                      void *stream);
 int fl_cusparse_destroy(fl_cusparse_t h);
+/* The two comparators on host buffers (device memory internal to the call):
+ * y = A x, *mean_ms = mean kernel time over `reps` launches (CUDA events,
+ * y zeroing outside the timed region).  CSC in original column order for the
+ * naive kernel, CSR for cuSPARSE (CUSPARSE_SPMV_ALG_DEFAULT). */
+int fl_csc_spmv_naive_host(int m, int n, int nnz, const int *csc_ptr,
+                           const int *csc_rowidx, const double *csc_val,
+                           const double *x, double *y, int reps,
+                           double *mean_ms);
+int fl_cusparse_spmv_host(int m, int n, int nnz, const int *csr_rowptr,
+                          const int *csr_colidx, const double *csr_val,
+                          const double *x, double *y, int reps,
+                          double *mean_ms);
 
 /* ---- storage / right-hand-side forms ---------------------------------- */
 

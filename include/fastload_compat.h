@@ -91,4 +91,35 @@ inline void FastLoad_spmv(char *filename, slide_matrix *matrix, int nnz, int col
 inline void Tile_destroy(slide_matrix *matrix) { fl_tile_destroy(matrix); }
 #endif
 
+/* mmio_allinone (src/auxiliary.h:64-232) with the entries parsed on the GPU.
+ * The reference defines mmio_allinone itself in auxiliary.h, so the shim has
+ * its own name and the reference's signature and return convention (0 on
+ * success, nonzero on failure); main.cu:40 switches by renaming the call. */
+inline int mmio_allinone_gpu(int *m, int *n, int *nnz, int *isSymmetric, int **csrrowptr, int **csrcolidx,
+                             double **csrval, char *filename) {
+    int rc = fl_mmio_allinone(m, n, nnz, isSymmetric, csrrowptr, csrcolidx, csrval, filename);
+    fastload_compat_detail::report("mmio_allinone", rc);
+    return rc;
+}
+
+/* The reference's comparators on host buffers (src/CSCSpMV.h:29-141,
+ * src/cusparse_cuda.h:27-155): y = A x with the naive CSC kernel or cuSPARSE
+ * CSR, device memory internal to the call, the mean kernel time in ms over
+ * `reps` launches (CUDA events) returned, or a negative value on error. */
+inline double csc_spmv_gpu_ms(int m, int n, int nnz, const int *csc_ptr, const int *csc_rowidx,
+                              const double *csc_val, const double *x, double *y, int reps) {
+    double ms = -1.0;
+    int rc = fl_csc_spmv_naive_host(m, n, nnz, csc_ptr, csc_rowidx, csc_val, x, y, reps, &ms);
+    fastload_compat_detail::report("csc_spmv", rc);
+    return rc == FL_SUCCESS ? ms : -1.0;
+}
+
+inline double cusparse_spmv_gpu_ms(int nnz, int rows, int cols, const int *csr_offsets, const int *csr_columns,
+                                   const double *csr_values, const double *x, double *y, int reps) {
+    double ms = -1.0;
+    int rc = fl_cusparse_spmv_host(rows, cols, nnz, csr_offsets, csr_columns, csr_values, x, y, reps, &ms);
+    fastload_compat_detail::report("cusparse_spmv", rc);
+    return rc == FL_SUCCESS ? ms : -1.0;
+}
+
 #endif

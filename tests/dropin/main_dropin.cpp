@@ -4,6 +4,7 @@
 // colidx) instead of a .mtx, then does what main.cu does: values i%10,
 // csr_to_csc, x = i%10, CSR and CSC goldens, ColSort, formatTransform, the
 // tile-order CPU check, FastLoad_spmv against the CSR golden, Tile_destroy.
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -16,15 +17,33 @@ int main(int argc, char **argv) {
         printf("error order\n");
         return 2;
     }
-    FILE *f = fopen(argv[1], "rb");
-    if (!f) return 2;
-    int hdr[3];
-    if (fread(hdr, sizeof(int), 3, f) != 3) return 2;
-    int rowA = hdr[0], colA = hdr[1], nnz = hdr[2];
-    std::vector<int> csrrowptr(rowA + 1), csrcolidx(nnz);
-    if (fread(csrrowptr.data(), sizeof(int), rowA + 1, f) != (size_t)rowA + 1) return 2;
-    if (fread(csrcolidx.data(), sizeof(int), nnz, f) != (size_t)nnz) return 2;
-    fclose(f);
+    int rowA = 0, colA = 0, nnz = 0;
+    std::vector<int> csrrowptr, csrcolidx;
+    const size_t len = strlen(argv[1]);
+    if (len > 4 && strcmp(argv[1] + len - 4, ".mtx") == 0) {
+        // main.cu:40, with the entries parsed on the GPU
+        int isSymmetricA = 0, *rp = nullptr, *ci = nullptr;
+        double *v = nullptr;
+        if (mmio_allinone_gpu(&rowA, &colA, &nnz, &isSymmetricA, &rp, &ci, &v, argv[1]) != 0) return 3;
+        csrrowptr.assign(rp, rp + rowA + 1);
+        csrcolidx.assign(ci, ci + nnz);
+        free(rp);
+        free(ci);
+        free(v);
+    } else {
+        FILE *f = fopen(argv[1], "rb");
+        if (!f) return 2;
+        int hdr[3];
+        if (fread(hdr, sizeof(int), 3, f) != 3) return 2;
+        rowA = hdr[0];
+        colA = hdr[1];
+        nnz = hdr[2];
+        csrrowptr.resize(rowA + 1);
+        csrcolidx.resize(nnz);
+        if (fread(csrrowptr.data(), sizeof(int), rowA + 1, f) != (size_t)rowA + 1) return 2;
+        if (fread(csrcolidx.data(), sizeof(int), nnz, f) != (size_t)nnz) return 2;
+        fclose(f);
+    }
     std::vector<double> csrval(nnz);
     for (int i = 0; i < nnz; i++) csrval[i] = i % 10;  // main.cu:68-69
     printf("read success,input matrix A :(%i,%i) nnz =%i  \n", rowA, colA, nnz);
@@ -78,6 +97,23 @@ int main(int argc, char **argv) {
     std::fill(y.begin(), y.end(), 0.0);
     char name[] = "dropin";
     FastLoad_spmv(name, matrixA, nnz, colA, rowA, sortx.data(), y.data(), y_goldencsr.data());
+
+    // the reference's comparators (CSCSpMV.h: 1% check; cusparse_cuda.h: exact check)
+    std::vector<double> yc(rowA, 0.0);
+    const double ms_csc = csc_spmv_gpu_ms(rowA, colA, nnz, csccolptr.data(), cscrowidx.data(), cscval.data(),
+                                          x.data(), yc.data(), 100);
+    int bad_csc = ms_csc < 0;
+    for (int i = 0; i < rowA && !bad_csc; i++)
+        if (std::abs(y_goldencsr[i] - yc[i]) > 0.01 * std::abs(yc[i])) bad_csc++;
+    if (!bad_csc) printf("BASIC CSC GPU PASS! (%f ms %4.2f GFlops)\n", ms_csc, 2.0 * nnz * 1.0e-6 / ms_csc);
+    else printf("BASIC CSC check NO PASS! error_count_cuda = %d \n", bad_csc);
+    std::vector<double> ys(rowA, 0.0);
+    const double ms_cs = cusparse_spmv_gpu_ms(nnz, rowA, colA, csrrowptr.data(), csrcolidx.data(), csrval.data(),
+                                              x.data(), ys.data(), 10);
+    bool ok_cs = ms_cs >= 0;
+    for (int i = 0; i < rowA && ok_cs; i++) ok_cs = ys[i] == y_goldencsr[i];
+    if (ok_cs) printf("cuSPARSE test PASSED! (%f ms %4.2f GFlops)\n", ms_cs, 2.0 * nnz * 1.0e-6 / ms_cs);
+    else printf("cuSPARSE test FAILED: wrong result\n");
     int exact = 0;
     for (int i = 0; i < rowA; i++) exact += y[i] == y_goldencsr[i];
     printf("exact %d of %d\n", exact, rowA);

@@ -177,6 +177,14 @@ def test_dropin_driver_runs_the_main_cu_sequence(gpu, tmp_path):
     assert "Check FASTLOAD GPU PASS!" in r.stdout
     assert "Check FASTLOAD CPU PASS!" in r.stdout
     assert f"tilenum {g['tilenum']}" in r.stdout
+    assert "BASIC CSC GPU PASS!" in r.stdout
+    assert "cuSPARSE test PASSED!" in r.stdout
+    # main.cu:40's read of a .mtx file, parsed on the GPU
+    mtx = os.path.join(ROOT, "tests", "golden", "mtx", "real_symmetric.mtx")
+    r = subprocess.run([exe, mtx], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "nnz =13" in r.stdout
+    assert "Check FASTLOAD GPU PASS!" in r.stdout and "Check FASTLOAD CPU PASS!" in r.stdout
 
 
 @pytest.mark.parametrize("name", golden_names())
