@@ -51,6 +51,24 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+def world_max(x: float, dist, device: str) -> float:
+    """Max of x over the ranks (the slowest replica sets the job's time);
+    x itself without a process group.  device: "cuda" for NCCL, "cpu" for gloo."""
+    if not dist:
+        return float(x)
+    import torch
+
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(bytes_per_step: float, world: int, ms_per_step: float) -> float:
+    """Whole-job GB/s of `world` independent replicas, each moving
+    bytes_per_step per step, timed by the slowest rank."""
+    return bytes_per_step * world / (ms_per_step * 1e-3) / 1e9
+
+
 def ncu_traffic(kernel, workload):
     """Per-launch DRAM bytes of `kernel` from the committed ncu summary
     (profiles/ncu_traffic.txt: '<kernel> <workload> <bytes>' lines)."""
@@ -159,7 +177,7 @@ def run_reference(args, rank, world):
         return
     import oracle
 
-    c = make_workload(args.n)
+    c = make_workload(args.cols)
     lay = oracle.build(c.m, c.n, csc=(c.colptr, c.rowidx, c.val), x=c.x)
     T = int(lay["tilenum"])
     # each step: a bounded, rotating sample of about 1/16 of the tiles
@@ -421,7 +439,7 @@ def run_gpu(args, rank, world):
         import torch.distributed as dist
 
         dist.init_process_group("nccl")
-    c = make_workload(args.n)
+    c = make_workload(args.cols)
     m, n, nnz = c.m, c.n, c.nnz
     B = algorithmic_bytes(m, n, nnz)
     stream = torch.cuda.current_stream()
@@ -467,13 +485,10 @@ def run_gpu(args, rank, world):
         dist.barrier()
     total_ms = start.elapsed_time(end)
     kern_ms = float(np.mean([a.elapsed_time(b) for a, b in ev]))
-    if dist:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = world_max(total_ms, dist, "cuda")
     ms_step = total_ms / K
     peak, peak_kind = measured_peaks()
-    value = B * world / (ms_step * 1e-3) / 1e9
+    value = replica_value(B, world, ms_step)
     achieved = B / (kern_ms * 1e-3) / 1e9
 
     # the reference-design kernel (one warp per tile) on the same inputs
@@ -562,7 +577,7 @@ def main():
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="fastload", choices=["fastload", "reference"])
-    ap.add_argument("--n", type=int, default=N_COLS, help="columns of the Zipf matrix (default 1,048,576)")
+    ap.add_argument("--cols", type=int, default=N_COLS, help="columns of the Zipf matrix (default 1,048,576)")
     ap.add_argument("--profile", default=None, help="case:values:band:k -- run one kernel for a profiler")
     ap.add_argument("--no-forms", action="store_true", help="skip the storage / multi-RHS form measurements")
     ap.add_argument("--no-compare", action="store_true", help="skip the naive-CSC and cuSPARSE comparator lines")
