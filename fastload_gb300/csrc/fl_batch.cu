@@ -1,13 +1,14 @@
-// fl_batch.cu -- many matrices through one persistent FastLoad launch.
+// fl_batch.cu -- many matrices through one persistent launch.
 //
-// A batch concatenates the FastLoad layouts of independent matrices: their
-// tile-ordered streams (rows shifted by each matrix's offset in the stacked
-// y, values converted to the storage type), their region tables (stream
-// starts and first sorted columns shifted into the stacked x) and their work
-// items.  One launch of the streaming form kernel then walks every matrix's
-// work items with the dynamic work counter, so matrices of very different
-// sizes share the GPU evenly.  fl_batch_spmv_graph captures the y zeroing,
-// the counter reset and the launch into a CUDA graph once and replays it.
+// A batch stacks every matrix as row slices: each matrix's rows are put into
+// the heavy-band layout with the band holding all of its columns (rows
+// sorted by length, 32 rows per slice, one lane per row), the slices of all
+// matrices are concatenated with rows shifted into the stacked y and columns
+// into the stacked (sorted) x, and the stacked slices are cut into work
+// units.  One launch of the form kernel then runs every matrix with each row
+// owned by one lane: no atomics, y stored once per row (rows without
+// nonzeros are zeroed first when there are any).  fl_batch_spmv_graph
+// captures the launch into a CUDA graph once and replays it.
 #include "fl_forms.cuh"
 
 #include <cstring>
@@ -28,12 +29,13 @@ struct fl_batch {
     int count = 0, vtype = FL_VALUES_F32, yf32 = 1;
     long M = 0, N = 0, NNZ = 0;
     std::vector<int> m_off, n_off;  // count+1 each
-    DevBuf<int> row;
-    DevBuf<unsigned char> val;
-    DevBuf<RegionDesc> regions;
-    DevBuf<ItemDesc> items;
-    int nitems = 0;
-    DevBuf<int> perm;  // stacked sorted position -> stacked original column
+    // stacked row slices
+    int nslices = 0, nunits = 0;
+    bool all_rows = false;        // every row of the batch has a nonzero
+    DevBuf<unsigned char> val;    // slice entries in the storage type
+    DevBuf<int> col;              // stacked sorted column of each entry
+    DevBuf<int> slice_ptr, srow, slen, unit_slice;
+    DevBuf<int> perm;             // stacked sorted position -> stacked original column
     DevBuf<int> err;
     // captured graph and the pointers it was captured with
     cudaGraphExec_t exec = nullptr;
@@ -54,9 +56,16 @@ int grid_b(long n, int threads) {
     return (int)std::max<long>(1, std::min(b, cap));
 }
 
-__global__ void k_batch_rows(const int *src, long n, int off, int *dst) {
+__global__ void k_stack_rows(const int *src, long n, int off, int *dst) {
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        const int r = src[i];
+        dst[i] = r < 0 ? -1 : r + off;
+    }
+}
+
+__global__ void k_stack_cols(const uint16_t *c16, const int *c32, long n, int off, int *dst) {
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
-        dst[i] = src[i] + off;
+        dst[i] = (c16 ? (int)c16[i] : c32[i]) + off;
 }
 
 __global__ void k_batch_vals(const double *src, long n, int vtype, unsigned char *dst) {
@@ -74,11 +83,6 @@ __global__ void k_batch_vals(const double *src, long n, int vtype, unsigned char
     }
 }
 
-__global__ void k_batch_fill(int *row, long from, long to) {
-    for (long i = from + blockIdx.x * (long)blockDim.x + threadIdx.x; i < to; i += (long)gridDim.x * blockDim.x)
-        row[i] = -1;
-}
-
 __global__ void k_batch_permute(const int *perm, long n, const double *x, float *xs32, double *xs64) {
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
         const double v = x[perm[i]];
@@ -91,55 +95,58 @@ size_t vsize(int vtype) { return vtype == FL_VALUES_F64 ? 8 : 4; }
 
 int launch(fl_batch *b, const void *xs, void *y, cudaStream_t s) {
     const size_t ysz = b->yf32 ? sizeof(float) : sizeof(double);
-    if (b->M) FL_CUDA(cudaMemsetAsync(y, 0, (size_t)b->M * ysz, s));
-    if (b->nitems == 0) return FL_SUCCESS;
+    if (b->M && !b->all_rows) FL_CUDA(cudaMemsetAsync(y, 0, (size_t)b->M * ysz, s));
+    if (b->nunits == 0) return FL_SUCCESS;
     auto fill = [&](auto &a) {
-        a.items = b->items.get();
-        a.regions = b->regions.get();
-        a.row = b->row.get();
-        a.nitems = b->nitems;
+        a.items = nullptr;
+        a.regions = nullptr;
+        a.row = nullptr;
+        a.val = nullptr;
+        a.nitems = 0;
         a.H0 = 0;
-        a.nh = 0;
-        a.nslices = 0;
-        a.nunits = 0;
+        a.nh = (int)std::max<long>(b->N, 1);
+        a.nslices = b->nslices;
+        a.nunits = b->nunits;
         a.bulk = 0;
-        a.heavy_mode = 0;
-        a.slice_ptr = a.hrow = a.hlen = a.unit_slice = nullptr;
-        a.hval = nullptr;
+        a.heavy_mode = 2;  // every row with nonzeros is owned by one lane
+        a.slice_ptr = b->slice_ptr.get();
+        a.hrow = b->srow.get();
+        a.hlen = b->slen.get();
+        a.unit_slice = b->unit_slice.get();
         a.hcol16 = nullptr;
-        a.hcol32 = nullptr;
+        a.hcol32 = b->col.get();
         a.err = b->err.get();
     };
     if (b->vtype == FL_VALUES_F64) {
         FormArgs<double, double> a;
         fill(a);
-        a.val = (const double *)b->val.get();
+        a.hval = (const double *)b->val.get();
         a.xs = (const double *)xs;
         a.y = (double *)y;
-        return run_form_f64(a, 1, false, s);
+        return run_form_f64(a, 1, true, s);
     }
     if (b->vtype == FL_VALUES_F32 && b->yf32) {
         FormArgs<float, float> a;
         fill(a);
-        a.val = (const float *)b->val.get();
+        a.hval = (const float *)b->val.get();
         a.xs = (const float *)xs;
         a.y = (float *)y;
-        return run_form_f32_y32(a, 1, false, s);
+        return run_form_f32_y32(a, 1, true, s);
     }
     if (b->vtype == FL_VALUES_F32) {
         FormArgs<float, double> a;
         fill(a);
-        a.val = (const float *)b->val.get();
+        a.hval = (const float *)b->val.get();
         a.xs = (const float *)xs;
         a.y = (double *)y;
-        return run_form_f32(a, 1, false, s);
+        return run_form_f32(a, 1, true, s);
     }
     FormArgs<bf16x2_t, double> a;
     fill(a);
-    a.val = (const bf16x2_t *)b->val.get();
+    a.hval = (const bf16x2_t *)b->val.get();
     a.xs = (const float *)xs;
     a.y = (double *)y;
-    return run_form_bf16(a, 1, false, s);
+    return run_form_bf16(a, 1, true, s);
 }
 
 }  // namespace
@@ -160,71 +167,100 @@ int fl_batch_create(fl_batch_t *out, int count, const fl_plan_t *plans, int valu
     b->yf32 = y_f32 != 0;
     b->m_off.assign(count + 1, 0);
     b->n_off.assign(count + 1, 0);
-    std::vector<long> e_off(count + 1, 0);
-    std::vector<int> r_off(count + 1, 0), i_off(count + 1, 0);
     for (int i = 0; i < count; i++) {
         if (!plans[i]) return fail(FL_ERR_ARG, "batch_create: plan %d is NULL", i);
         const Layout &L = plans[i]->L;
-        b->m_off[i + 1] = b->m_off[i] + L.m;
-        b->n_off[i + 1] = b->n_off[i] + L.n;
-        e_off[i + 1] = e_off[i] + L.nnz;
-        r_off[i + 1] = r_off[i] + L.regions.nregions;
-        i_off[i + 1] = i_off[i] + L.regions.nitems;
-        if ((long)b->m_off[i + 1] != (long)b->m_off[i] + L.m || e_off[i + 1] > 0x7fffffffL - 65536)
+        const long mo = (long)b->m_off[i] + L.m, no = (long)b->n_off[i] + L.n;
+        b->NNZ += L.nnz;
+        if (mo > 0x7fffffffL || no > 0x7fffffffL || b->NNZ > 0x7fffffffL)
             return fail(FL_ERR_OVERFLOW, "batch_create: the stacked batch exceeds the 32-bit index space");
+        b->m_off[i + 1] = (int)mo;
+        b->n_off[i + 1] = (int)no;
     }
     b->M = b->m_off[count];
     b->N = b->n_off[count];
-    b->NNZ = e_off[count];
-    b->nitems = i_off[count];
-    cudaStream_t s = 0;
+    const cudaStream_t s = 0;
     FL_CUDA(cudaDeviceSynchronize());
-    const size_t np = padded((size_t)b->NNZ);
-    FL_TRY(b->row.alloc(np, s));
-    FL_TRY(b->val.alloc(np * vsize(value_type), s));
-    FL_CUDA(cudaMemsetAsync(b->val.get(), 0, np * vsize(value_type), s));
-    k_batch_fill<<<grid_b(np - b->NNZ, 256), 256, 0, s>>>(b->row.get(), b->NNZ, (long)np);
-    FL_CUDA(cudaGetLastError());
-    std::vector<RegionDesc> reg(std::max(r_off[count], 1));
-    std::vector<ItemDesc> itm(std::max(i_off[count], 1));
-    std::vector<int> perm(std::max<long>(b->N, 1));
+    // each matrix's rows as slices with every column in the band, built one
+    // matrix at a time and appended to the stacked arrays
+    std::vector<Bucket> parts(count);
+    std::vector<long> e_off(count + 1, 0);
+    std::vector<int> s_off(count + 1, 0);
+    long rows_covered = 0;
     for (int i = 0; i < count; i++) {
         const Layout &L = plans[i]->L;
         if (L.nnz) {
-            k_batch_rows<<<grid_b(L.nnz, 256), 256, 0, s>>>(L.row.get(), L.nnz, b->m_off[i], b->row.get() + e_off[i]);
-            FL_CUDA(cudaGetLastError());
-            k_batch_vals<<<grid_b(L.nnz, 256), 256, 0, s>>>(L.val.get(), L.nnz, value_type,
-                                                             b->val.get() + e_off[i] * vsize(value_type));
-            FL_CUDA(cudaGetLastError());
+            DevBuf<int> srow;
+            DevBuf<double> sval;
+            FL_TRY(untile_layout(L, srow, sval, s));
+            FL_TRY(build_bucket(parts[i], L.m, L.n, L.nnz, L.sortnnz.get(), srow.get(), sval.get(), L.n, s, true));
         }
-        if (L.regions.nregions)
-            FL_CUDA(cudaMemcpyAsync(reg.data() + r_off[i], L.regions.region.get(),
-                                    L.regions.nregions * sizeof(RegionDesc), cudaMemcpyDeviceToHost, s));
-        if (L.regions.nitems)
-            FL_CUDA(cudaMemcpyAsync(itm.data() + i_off[i], L.regions.item.get(), L.regions.nitems * sizeof(ItemDesc),
+        const HeavyBand &H = parts[i].heavy;
+        const int ns = L.nnz ? H.nslices : 0;
+        e_off[i + 1] = e_off[i] + (L.nnz ? H.padded : 0);
+        if ((long)s_off[i] + ns > 0x7fffffffL / 32 || e_off[i + 1] > 0x7fffffffL)
+            return fail(FL_ERR_OVERFLOW, "batch_create: the stacked slices exceed the 32-bit index space");
+        s_off[i + 1] = s_off[i] + ns;
+        rows_covered += L.nnz ? H.nrows : 0;
+        parts[i].light = Layout();  // band holds every column: no light part
+    }
+    b->nslices = s_off[count];
+    b->all_rows = rows_covered == b->M;
+    const long E = std::max<long>(e_off[count], 1);
+    FL_TRY(b->val.alloc((size_t)E * vsize(value_type), s));
+    FL_TRY(b->col.alloc(E, s));
+    FL_TRY(b->slice_ptr.alloc((size_t)b->nslices + 1, s));
+    FL_TRY(b->srow.alloc(std::max(32L * b->nslices, 1L), s));
+    FL_TRY(b->slen.alloc(std::max(32L * b->nslices, 1L), s));
+    std::vector<int> sp((size_t)b->nslices + 1, 0), perm(std::max<long>(b->N, 1));
+    for (int i = 0; i < count; i++) {
+        const Layout &L = plans[i]->L;
+        const HeavyBand &H = parts[i].heavy;
+        const int ns = s_off[i + 1] - s_off[i];
+        if (ns) {
+            const long ne = e_off[i + 1] - e_off[i];
+            k_batch_vals<<<grid_b(ne, 256), 256, 0, s>>>(H.val.get(), ne, value_type,
+                                                          b->val.get() + e_off[i] * vsize(value_type));
+            FL_CUDA(cudaGetLastError());
+            k_stack_cols<<<grid_b(ne, 256), 256, 0, s>>>(H.col.get(), H.col.get() ? nullptr : H.col32.get(), ne,
+                                                          b->n_off[i], b->col.get() + e_off[i]);
+            FL_CUDA(cudaGetLastError());
+            k_stack_rows<<<grid_b(32L * ns, 256), 256, 0, s>>>(H.row.get(), 32L * ns, b->m_off[i],
+                                                                b->srow.get() + 32L * s_off[i]);
+            FL_CUDA(cudaGetLastError());
+            FL_CUDA(cudaMemcpyAsync(b->slen.get() + 32L * s_off[i], H.len.get(), 32L * ns * sizeof(int),
+                                    cudaMemcpyDeviceToDevice, s));
+            FL_CUDA(cudaMemcpyAsync(sp.data() + s_off[i], H.slice_ptr.get(), (size_t)ns * sizeof(int),
                                     cudaMemcpyDeviceToHost, s));
+        }
         if (L.n)
             FL_CUDA(cudaMemcpyAsync(perm.data() + b->n_off[i], L.perm.get(), L.n * sizeof(int), cudaMemcpyDeviceToHost,
                                     s));
+        FL_CUDA(cudaStreamSynchronize(s));
+        parts[i] = Bucket();  // release this matrix's band before the next
     }
-    FL_CUDA(cudaStreamSynchronize(s));
     for (int i = 0; i < count; i++) {
-        for (int r = r_off[i]; r < r_off[i + 1]; r++) {
-            reg[r].start += (int)e_off[i];
-            reg[r].col_base += b->n_off[i];
-        }
-        for (int t = i_off[i]; t < i_off[i + 1]; t++) {
-            itm[t].begin += (int)e_off[i];
-            itm[t].end += (int)e_off[i];
-            itm[t].region += r_off[i];
-        }
+        for (int q = s_off[i]; q < s_off[i + 1]; q++) sp[q] += (int)e_off[i];
         for (int c = b->n_off[i]; c < b->n_off[i + 1]; c++) perm[c] += b->n_off[i];
     }
-    FL_TRY(b->regions.alloc(reg.size(), s));
-    FL_TRY(b->items.alloc(itm.size(), s));
+    sp[b->nslices] = (int)e_off[count];
+    // work units: runs of consecutive stacked slices, about four per
+    // resident warp (never less than one slice)
+    std::vector<int> ub(1, 0);
+    const long per_unit = std::max<long>(1, e_off[count] / (4L * num_sms() * 32));
+    long acc = 0;
+    for (int q = 0; q < b->nslices; q++) {
+        acc += sp[q + 1] - sp[q];
+        if (acc >= per_unit || q == b->nslices - 1) {
+            ub.push_back(q + 1);
+            acc = 0;
+        }
+    }
+    b->nunits = (int)ub.size() - 1;
+    FL_TRY(b->unit_slice.alloc(ub.size(), s));
     FL_TRY(b->perm.alloc(perm.size(), s));
-    FL_CUDA(cudaMemcpyAsync(b->regions.get(), reg.data(), reg.size() * sizeof(RegionDesc), cudaMemcpyHostToDevice, s));
-    FL_CUDA(cudaMemcpyAsync(b->items.get(), itm.data(), itm.size() * sizeof(ItemDesc), cudaMemcpyHostToDevice, s));
+    FL_CUDA(cudaMemcpyAsync(b->slice_ptr.get(), sp.data(), sp.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+    FL_CUDA(cudaMemcpyAsync(b->unit_slice.get(), ub.data(), ub.size() * sizeof(int), cudaMemcpyHostToDevice, s));
     FL_CUDA(cudaMemcpyAsync(b->perm.get(), perm.data(), perm.size() * sizeof(int), cudaMemcpyHostToDevice, s));
     FL_TRY(b->err.alloc(1, s));
     FL_CUDA(cudaMemsetAsync(b->err.get(), 0, sizeof(int), s));
@@ -240,7 +276,7 @@ int fl_batch_info(fl_batch_t b, int *count, long *m_total, long *n_total, long *
     if (m_total) *m_total = b->M;
     if (n_total) *n_total = b->N;
     if (nnz_total) *nnz_total = b->NNZ;
-    if (items) *items = b->nitems;
+    if (items) *items = b->nunits;
     return FL_SUCCESS;
 }
 

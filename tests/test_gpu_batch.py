@@ -60,3 +60,30 @@ def test_batch_rejects_bad_arguments(gpu):
     plans = [gpu.Plan.from_csc(c.m, c.n, c.colptr, c.rowidx, c.val) for c in mats]
     with pytest.raises(gpu.FastLoadError):
         gpu.Batch(plans, value_type=2, y_f32=True)
+
+
+@pytest.mark.parametrize("empty_rows", [False, True])
+def test_batch_overwrites_stale_y(gpu, empty_rows):
+    """Rows are owned by one lane and stored, not accumulated: whatever y held
+    before (here NaN) is replaced, including rows without nonzeros."""
+    import torch
+
+    from fastload_gb300 import gen
+
+    mats = [gen.diag_poisson(n, seed=n) for n in (300, 1000, 77)]
+    if empty_rows:
+        mats.append(gen.from_csr_lists(6, 4, [(0, 0, 1.5), (2, 1, -2.0), (2, 3, 3.0), (5, 2, 4.0)],
+                                       x=np.arange(4.0)))  # rows 1, 3, 4 empty
+    plans = [gpu.Plan.from_csc(c.m, c.n, c.colptr, c.rowidx, c.val) for c in mats]
+    with gpu.Batch(plans, value_type=0, y_f32=False) as b:
+        x = torch.from_numpy(np.concatenate([c.x for c in mats])).cuda()
+        xs = b.permute_x(x)
+        for run in (b.spmv, b.spmv_graph):
+            y = torch.full((b.m,), float("nan"), dtype=torch.float64, device="cuda")
+            yy = run(xs, y).cpu().numpy()
+            assert np.isfinite(yy).all()
+            for i, c in enumerate(mats):
+                ref = oracle.csc_spmv_dd(c.m, c.n, c.colptr, c.rowidx, c.val, c.x)
+                assert oracle.rel_errors(yy[b.m_off[i]:b.m_off[i + 1]], ref)[0] <= 1e-12
+    for p in plans:
+        p.close()
