@@ -224,6 +224,15 @@ class Plan:
         check(load().fl_plan_add_form(self._h, int(value_type), int(heavy_band), int(y_f32), C.byref(fid)))
         return fid.value
 
+    def add_tuned_form(self, value_type: int = VALUES_F32, y_f32: bool = False, model=None) -> tuple[int, str]:
+        """Adds a form whose heavy band the learned tuner picks for this
+        matrix (tuner.choose: the plan's features through the trained MLP on
+        the GPU).  Returns (form id, chosen variant)."""
+        from . import tuner
+
+        variant, band = tuner.choose(self, value_type, model)
+        return self.add_form(value_type, band, y_f32=y_f32), variant
+
     def form_info(self, form_id: int) -> dict:
         i = FormInfoC()
         check(load().fl_plan_form_info(self._h, int(form_id), C.byref(i)))

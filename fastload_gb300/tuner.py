@@ -24,6 +24,7 @@ fallback and the judge of regret.
 from __future__ import annotations
 
 import argparse
+import os
 import ctypes as C
 import json
 import time
@@ -256,6 +257,45 @@ class Network:
             pass
 
 
+MODEL = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tuner_data", "model.npz")
+
+
+def save_model(net: Network, path: str) -> None:
+    """Weights, feature scaling, shape and variant names of a trained network."""
+    np.savez_compressed(path, params=net.params(), mu=net.mu, sd=net.sd, shape=np.array(net.shape),
+                        variants=np.array(VARIANTS))
+
+
+def load_model(path: str = MODEL) -> Network:
+    """The trained network of `path` on the current device."""
+    with np.load(path) as z:
+        shape = tuple(int(v) for v in z["shape"])
+        if tuple(str(v) for v in z["variants"]) != VARIANTS:
+            raise ValueError(f"{path}: variants {list(z['variants'])} differ from {list(VARIANTS)}")
+        net = Network(*shape)
+        net.set_params(z["params"])
+        net.mu = z["mu"].astype(np.float32)
+        net.sd = z["sd"].astype(np.float32)
+    return net
+
+
+_LOADED: dict = {}
+
+
+def choose(plan, value_type: int, model: str | None = None) -> tuple[str, int]:
+    """(variant, heavy band) the trained network predicts fastest for this
+    plan's matrix in the given value type."""
+    path = model or MODEL
+    net = _LOADED.get(path)
+    if net is None:
+        net = _LOADED[path] = load_model(path)
+    v = VARIANTS[int(net.predict(features(plan, value_type)[None, :])[0])]
+    band = variant_band(v, value_type)
+    if band > plan.n:
+        band = variant_band("all", value_type)
+    return v, band
+
+
 def targets(times) -> np.ndarray:
     """log2(t_variant / t_best) per matrix: 0 for the best variant."""
     t = np.asarray(times, np.float64)
@@ -304,6 +344,12 @@ def main():
     c.add_argument("--count", type=int, default=2200)
     c.add_argument("--seed", type=int, default=5)
     c.add_argument("--out", required=True)
+    t = sub.add_parser("train", help="train on the first --train matrices and save the model")
+    t.add_argument("--data", required=True)
+    t.add_argument("--train", type=int, default=2000)
+    t.add_argument("--epochs", type=int, default=3000)
+    t.add_argument("--seed", type=int, default=1)
+    t.add_argument("--out", default=MODEL)
     e = sub.add_parser("evaluate")
     e.add_argument("--data", required=True)
     e.add_argument("--train", type=int, default=2000)
@@ -311,9 +357,20 @@ def main():
     a = ap.parse_args()
     if a.cmd == "collect":
         collect(a.count, a.seed, a.out)
+        return
+    with np.load(a.data) as z:
+        data = {k: z[k] for k in z.files}
+    if a.cmd == "train":
+        X, T = np.asarray(data["X"]), np.asarray(data["T"])
+        net = Network(seed=a.seed)
+        losses = net.fit(X[:a.train], T[:a.train], epochs=a.epochs)
+        save_model(net, a.out)
+        res = {"train": evaluate(net.predict(X[:a.train]), T[:a.train]),
+               "heldout": evaluate(net.predict(X[a.train:]), T[a.train:]) if len(X) > a.train else None,
+               "final_loss": float(losses[-1]), "model": a.out}
+        net.close()
+        print(json.dumps(res))
     else:
-        with np.load(a.data) as z:
-            data = {k: z[k] for k in z.files}
         print(json.dumps(train_and_evaluate(data, a.train, a.epochs)))
 
 

@@ -125,3 +125,46 @@ def test_trained_tuner_heldout_regret(gpu):
     assert h["matrices"] >= 150
     assert h["mean_regret"] <= 0.10, h
     assert h["speedup_vs_auto_rule"] >= 1.0, h
+
+
+MODEL = os.path.join(ROOT, "fastload_gb300", "tuner_data", "model.npz")
+
+
+@pytest.mark.skipif(not (os.path.exists(DATA) and os.path.exists(MODEL)), reason="trained model not committed")
+def test_tuned_form_follows_the_committed_model(gpu):
+    """Plan.add_tuned_form regenerates held-out matrices of the autotuner data
+    from their specs, picks the variant the committed model predicts from the
+    stored features, and the tuned form computes the product."""
+    import json
+
+    import torch
+
+    from fastload_gb300 import tuner
+
+    with np.load(DATA) as z:
+        X, metas = z["X"], [json.loads(m) for m in z["meta"]]
+    net = tuner.load_model(MODEL)
+    expect = net.predict(X)
+    net.close()
+    picked = 0
+    for i in range(2000, 2200):
+        spec = metas[i]
+        if spec["nnz"] > 3_000_000:
+            continue
+        plan, nnz, x = tuner.make_plan(spec)
+        try:
+            fid, variant = plan.add_tuned_form(spec["values"])
+            assert variant == tuner.VARIANTS[int(expect[i])], (i, variant)
+            xs = plan.permute_x_k(x, k=1, to_f32=spec["values"] != 0)
+            y = plan.spmv_form(fid, xs)
+            y0 = plan.spmv(plan.permute_x(x))
+            torch.cuda.synchronize()
+            rel = (torch.linalg.norm(y.double() - y0) / torch.linalg.norm(y0)).item()
+            assert rel <= (1e-12 if spec["values"] == 0 else 2e-5), (i, rel)
+            plan.check()
+        finally:
+            plan.close()
+        picked += 1
+        if picked == 12:
+            break
+    assert picked >= 6
