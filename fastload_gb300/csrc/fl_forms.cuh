@@ -194,7 +194,131 @@ __device__ __forceinline__ void heavy_unit(const FormArgs<V, Y> &a, int ub, int 
     }
 }
 
-template <typename V, int K, bool XS, bool C16, typename Y>
+// y[r] update of a finished row (atomic, read-modify-write or store).
+template <typename A, int K, typename Y>
+__device__ __forceinline__ void heavy_flush(int mode, Y *y, int r, const A acc[K]) {
+    Y *yr = y + (size_t)r * K;
+    if (mode == 0) {
+#pragma unroll
+        for (int q = 0; q < K; q++) atomicAdd(yr + q, (Y)acc[q]);
+    } else if (mode == 1) {
+#pragma unroll
+        for (int q = 0; q < K; q++) yr[q] += (Y)acc[q];
+    } else {
+#pragma unroll
+        for (int q = 0; q < K; q++) yr[q] = (Y)acc[q];
+    }
+}
+
+// ---- heavy band through a shared-memory ring (K = 1, x and columns narrow) --
+// A unit's slices are contiguous, so its values and 16-bit columns are one
+// run of 32-entry steps.  Each warp streams that run through a ring of
+// RING_STAGES stages of RING_STEPS steps in its own slice of shared memory
+// with cp.async (16-byte copies, completion tracked per thread by
+// cp.async.wait_group -- a hardware wait, no spin), so RING_STAGES-1 stages
+// are in flight while one is consumed, without holding registers.
+constexpr int RING_STEPS = 2;
+constexpr int RING_STAGES = 4;
+constexpr int SMEM_OPTIN = 232448;  // 227 KB: the largest dynamic shared memory of a block
+
+template <typename V>
+__host__ __device__ constexpr int ring_stage_bytes() {
+    return RING_STEPS * (32 * (int)sizeof(V) + 32 * (int)sizeof(uint16_t));
+}
+template <typename V>
+__host__ __device__ constexpr int ring_warp_bytes() {
+    return RING_STAGES * ring_stage_bytes<V>();
+}
+
+__device__ __forceinline__ void cp_async16(void *smem_dst, const void *gsrc) {
+    const uint32_t d = (uint32_t)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// Stage k (steps RING_STEPS*k ...) of the unit starting at entry E0 with T
+// steps into ring slot k % RING_STAGES; always commits a group (empty past
+// the end) so the per-thread group count stays in step with k.
+template <typename V>
+__device__ __forceinline__ void ring_issue(unsigned char *ring, const V *hval, const uint16_t *hcol, int E0, int T,
+                                           int k, int lane) {
+    const int t0 = k * RING_STEPS;
+    const int steps = min(RING_STEPS, T - t0);
+    if (steps > 0) {
+        unsigned char *slot = ring + (k % RING_STAGES) * ring_stage_bytes<V>();
+        const int vbytes = steps * 32 * (int)sizeof(V), cbytes = steps * 64;
+        const char *vsrc = (const char *)(hval + E0 + 32 * t0);
+        const char *csrc = (const char *)(hcol + E0 + 32 * t0);
+        for (int off = lane * 16; off < vbytes; off += 512) cp_async16(slot + off, vsrc + off);
+        unsigned char *cdst = slot + RING_STEPS * 32 * sizeof(V);
+        for (int off = lane * 16; off < cbytes; off += 512) cp_async16(cdst + off, csrc + off);
+    }
+    cp_async_commit();
+}
+
+template <typename V, typename Y>
+__device__ __forceinline__ void heavy_unit_ring(const FormArgs<V, Y> &a, int ub, int ue,
+                                                const typename VT<V>::X *xsrc, unsigned char *ring, int lane) {
+    using A = typename VT<V>::A;
+    if (ub >= ue) return;
+    const int E0 = __ldg(a.slice_ptr + ub);
+    const int T = (__ldg(a.slice_ptr + ue) - E0) >> 5;
+    const int nst = (T + RING_STEPS - 1) / RING_STEPS;
+#pragma unroll
+    for (int k = 0; k < RING_STAGES; k++) ring_issue<V>(ring, a.hval, a.hcol16, E0, T, k, lane);
+    int bnd = (__ldg(a.slice_ptr + ub + 1) - E0) >> 5;  // first step of the next slice
+    int len = __ldg(a.hlen + 32 * ub + lane), r = __ldg(a.hrow + 32 * ub + lane);
+    int nbnd = T, nlen = 0, nr = 0;
+    if (ub + 1 < ue) {
+        nbnd = (__ldg(a.slice_ptr + ub + 2) - E0) >> 5;
+        nlen = __ldg(a.hlen + 32 * (ub + 1) + lane);
+        nr = __ldg(a.hrow + 32 * (ub + 1) + lane);
+    }
+    int sl = ub, j = 0;
+    A acc[1] = {(A)0};
+    for (int k = 0; k < nst; k++) {
+        cp_async_wait<RING_STAGES - 1>();
+        __syncwarp();
+        const unsigned char *slot = ring + (k % RING_STAGES) * ring_stage_bytes<V>();
+        const V *sv = (const V *)slot;
+        const uint16_t *sc = (const uint16_t *)(slot + RING_STEPS * 32 * sizeof(V));
+#pragma unroll
+        for (int q = 0; q < RING_STEPS; q++) {
+            const int t = k * RING_STEPS + q;
+            if (t < T) {
+                if (j < len) {
+                    const A v = VT<V>::plain1(sv + 32 * q + lane);  // shared memory
+                    acc[0] = fma(v, (A)xsrc[sc[32 * q + lane]], acc[0]);
+                }
+                j++;
+                if (t + 1 == bnd) {
+                    if (len > 0) heavy_flush<A, 1, Y>(a.heavy_mode, a.y, r, acc);
+                    acc[0] = (A)0;
+                    sl++;
+                    j = 0;
+                    len = nlen;
+                    r = nr;
+                    bnd = nbnd;
+                    if (sl + 1 < ue) {
+                        nbnd = (__ldg(a.slice_ptr + sl + 2) - E0) >> 5;
+                        nlen = __ldg(a.hlen + 32 * (sl + 1) + lane);
+                        nr = __ldg(a.hrow + 32 * (sl + 1) + lane);
+                    }
+                }
+            }
+        }
+        __syncwarp();
+        ring_issue<V>(ring, a.hval, a.hcol16, E0, T, k + RING_STAGES, lane);
+    }
+    cp_async_wait<0>();
+    __syncwarp();
+}
+
+template <typename V, int K, bool XS, bool C16, typename Y, bool RING = false>
 __global__ void __launch_bounds__(FM_THREADS, 1) k_spmv_form(const FormArgs<V, Y> a) {
     using X = typename VT<V>::X;
     extern __shared__ __align__(128) unsigned char fm_smem[];
@@ -272,8 +396,13 @@ __global__ void __launch_bounds__(FM_THREADS, 1) k_spmv_form(const FormArgs<V, Y
             }
             staged = true;
         }
-        heavy_unit<V, K, XS, C16, Y>(a, __ldg(a.unit_slice + (u - a.nitems)), __ldg(a.unit_slice + (u - a.nitems) + 1),
-                                     xsrc, lane);
+        const int ub = __ldg(a.unit_slice + (u - a.nitems)), ue = __ldg(a.unit_slice + (u - a.nitems) + 1);
+        if constexpr (RING) {
+            const size_t xb = ((size_t)a.nh * K * sizeof(X) + 127) & ~(size_t)127;
+            heavy_unit_ring<V, Y>(a, ub, ue, xsrc, fm_smem + xb + (size_t)(tid >> 5) * ring_warp_bytes<V>(), lane);
+        } else {
+            heavy_unit<V, K, XS, C16, Y>(a, ub, ue, xsrc, lane);
+        }
     }
     if (XS && use_band && a.bulk && !staged) {
         bool ok = false;
@@ -292,9 +421,9 @@ __global__ void __launch_bounds__(FM_THREADS, 1) k_spmv_form(const FormArgs<V, Y
 }
 
 // Launch of one form kernel; xs/y typed per the form.
-template <typename V, int K, bool XS, bool C16, typename Y>
+template <typename V, int K, bool XS, bool C16, typename Y, bool RING = false>
 int launch_form(const FormArgs<V, Y> &a, size_t smem, cudaStream_t s) {
-    auto kern = k_spmv_form<V, K, XS, C16, Y>;
+    auto kern = k_spmv_form<V, K, XS, C16, Y, RING>;
     if (smem > 0) FL_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
     FL_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, FM_THREADS, smem));
@@ -314,6 +443,12 @@ int dispatch_form(const FormArgs<V, Y> &a, int k, bool wide_cols, cudaStream_t s
     const bool xs_smem = a.nh > 0 && !wide_cols && smem <= (size_t)FM_SMEM_MAX;
     const size_t dyn = xs_smem ? smem : 0;
     if (k == 1) {
+        // the heavy band through per-warp shared-memory rings when x and the
+        // rings fit beside each other
+        const size_t xb = (smem + 127) & ~(size_t)127;
+        const size_t ring = (size_t)(FM_THREADS / 32) * ring_warp_bytes<V>();
+        if (xs_smem && a.nslices > 0 && xb + ring <= (size_t)SMEM_OPTIN)
+            return launch_form<V, 1, true, true, Y, true>(a, xb + ring, s);
         if (xs_smem) return launch_form<V, 1, true, true, Y>(a, dyn, s);
         if (!wide_cols) return launch_form<V, 1, false, true, Y>(a, 0, s);
         return launch_form<V, 1, false, false, Y>(a, 0, s);

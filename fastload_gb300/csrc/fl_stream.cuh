@@ -50,6 +50,7 @@ struct VT<double> {
         return r;
     }
     static __device__ __forceinline__ A cached1(const double *p) { return __ldg(p); }
+    static __device__ __forceinline__ A plain1(const double *p) { return *p; }  // any address space
 };
 
 template <>
@@ -62,6 +63,7 @@ struct VT<float> {
         return r;
     }
     static __device__ __forceinline__ A cached1(const float *p) { return __ldg(p); }
+    static __device__ __forceinline__ A plain1(const float *p) { return *p; }  // any address space
 };
 
 template <>
@@ -75,6 +77,9 @@ struct VT<bf16x2_t> {
     }
     static __device__ __forceinline__ A cached1(const bf16x2_t *p) {
         return bf16x2_decode(__ldg((const unsigned *)p));
+    }
+    static __device__ __forceinline__ A plain1(const bf16x2_t *p) {  // any address space
+        return bf16x2_decode(*(const unsigned *)p);
     }
 };
 
