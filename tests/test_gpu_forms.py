@@ -132,3 +132,24 @@ def test_full_size_zipf_fp32_auto_band(gpu):
         assert p.form_info(fid)["heavy_cols"] > 0
         check(run_form(gpu, p, fid, 1, c.x, 1), yref, 1, False, "zipf/f32")
         p.check()
+
+
+@pytest.mark.parametrize("vtype", [0, 1, 2])
+def test_heavy_band_paths_agree(gpu, vtype):
+    """The three heavy-band paths on one matrix: a band whose x fits shared
+    memory beside the per-warp cp.async rings (16,384 columns), a band too
+    wide for the rings but not for shared memory (the register-pipelined
+    loop: 20,000 FP64 / 47,000 FP32 columns), and every column (x read from
+    global memory)."""
+    from fastload_gb300 import gen
+
+    c = gen.zipf_columns(60000, 1.5, 3000, seed=17)
+    yref = oracle.csc_spmv_dd(c.m, c.n, c.colptr, c.rowidx, c.val, c.x)
+    wide = 20000 if vtype == 0 else 47000
+    with gpu.Plan.from_csc(c.m, c.n, c.colptr, c.rowidx, c.val) as p:
+        for band in (16384, wide, gpu.BAND_ALL):
+            fid = p.add_form(vtype, band)
+            info = p.form_info(fid)
+            assert info["heavy_cols"] == (c.n if band == gpu.BAND_ALL else band)
+            check(run_form(gpu, p, fid, vtype, c.x, 1), yref, vtype, False, f"v{vtype}/band{band}")
+        p.check()
