@@ -15,8 +15,8 @@ column degrees, banded, block-diagonal, row-skewed) generated on the GPU
 (fl_gen_fill), n log-uniform in [1e4, 4e6], nnz log-uniform in [1e5, 6e7],
 FP64 or FP32 values.  The network (24 -> 64 -> 64 -> 6, ReLU) regresses
 log2(t_variant / t_best) and is trained on the GPU by the library's own
-forward/backward/Adam kernels (fl_mlp_*); the autotuner's measurement is the
-fallback and the judge of regret.
+forward/backward/Adam kernels (fl_mlp_*); the autotuner's measurements are
+what regret is measured against.
 
     python -m fastload_gb300.tuner collect --count 2200 --out data.npz
     python -m fastload_gb300.tuner evaluate --data data.npz
