@@ -25,7 +25,7 @@
 namespace fl {
 
 constexpr int BK_MAX_BAND = 24576;            // 192 KB of FP64 x in shared memory
-constexpr int BK_AUTO_BAND = 16384;           // default band width cap
+constexpr int BK_AUTO_BAND_BYTES = 131072;    // automatic band: at most 128 KB of x in shared memory
 constexpr int BK_AUTO_MIN_DEGREE = 32;        // densest columns worth a row slice
 
 int bucket_max_band() { return BK_MAX_BAND; }
@@ -97,9 +97,11 @@ static int bits_of(unsigned long v) {
     return b;
 }
 
-int bucket_auto_band(const int *sortnnz, int n, int nnz, cudaStream_t s) {
+int bucket_auto_band(const int *sortnnz, int n, int nnz, cudaStream_t s, int x_bytes) {
     if (n <= 0 || nnz <= 0) return 0;
-    const int tail = std::min(n, BK_AUTO_BAND);
+    // 16,384 columns of FP64 x, 32,768 of FP32 x: what fits 128 KB of shared
+    // memory beside the per-warp rings
+    const int tail = std::min(n, BK_AUTO_BAND_BYTES / std::max(x_bytes, 1));
     std::vector<int> h(tail);
     FL_TRY(read_ints(s, sortnnz + (n - tail), h.data(), tail));
     int band = 0;

@@ -240,7 +240,7 @@ int bucket_max_band();
 // Heavy band width chosen from the sorted column counts (device array):
 // the densest columns with at least `min_degree` nonzeros, at most the
 // shared-memory limit, or 0 when the band would hold little of the matrix.
-int bucket_auto_band(const int *sortnnz, int n, int nnz, cudaStream_t s);
+int bucket_auto_band(const int *sortnnz, int n, int nnz, cudaStream_t s, int x_bytes = 8);
 
 int num_sms();
 
