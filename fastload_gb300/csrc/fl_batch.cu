@@ -34,7 +34,8 @@ struct fl_batch {
     bool all_rows = false;        // every row of the batch has a nonzero
     DevBuf<unsigned char> val;    // slice entries in the storage type
     DevBuf<int> col;              // stacked sorted column of each entry
-    DevBuf<int> slice_ptr, srow, slen, unit_slice;
+    DevBuf<int> slice_ptr, srow, slen, unit_slice, unit_step;
+    bool split = false;           // a slice is cut across units (y by atomics)
     DevBuf<int> perm;             // stacked sorted position -> stacked original column
     DevBuf<int> err;
     // captured graph and the pointers it was captured with
@@ -95,7 +96,7 @@ size_t vsize(int vtype) { return vtype == FL_VALUES_F64 ? 8 : 4; }
 
 int launch(fl_batch *b, const void *xs, void *y, cudaStream_t s) {
     const size_t ysz = b->yf32 ? sizeof(float) : sizeof(double);
-    if (b->M && !b->all_rows) FL_CUDA(cudaMemsetAsync(y, 0, (size_t)b->M * ysz, s));
+    if (b->M && (!b->all_rows || b->split)) FL_CUDA(cudaMemsetAsync(y, 0, (size_t)b->M * ysz, s));
     if (b->nunits == 0) return FL_SUCCESS;
     auto fill = [&](auto &a) {
         a.items = nullptr;
@@ -108,11 +109,14 @@ int launch(fl_batch *b, const void *xs, void *y, cudaStream_t s) {
         a.nslices = b->nslices;
         a.nunits = b->nunits;
         a.bulk = 0;
-        a.heavy_mode = 2;  // every row with nonzeros is owned by one lane
+        // every row with nonzeros is owned by one lane, unless its slice is
+        // cut across units: then the parts meet in y by atomics
+        a.heavy_mode = b->split ? 0 : 2;
         a.slice_ptr = b->slice_ptr.get();
         a.hrow = b->srow.get();
         a.hlen = b->slen.get();
         a.unit_slice = b->unit_slice.get();
+        a.unit_step = b->unit_step.get();
         a.hcol16 = nullptr;
         a.hcol32 = b->col.get();
         a.err = b->err.get();
@@ -244,23 +248,18 @@ int fl_batch_create(fl_batch_t *out, int count, const fl_plan_t *plans, int valu
         for (int c = b->n_off[i]; c < b->n_off[i + 1]; c++) perm[c] += b->n_off[i];
     }
     sp[b->nslices] = (int)e_off[count];
-    // work units: runs of consecutive stacked slices, about four per
-    // resident warp (never less than one slice)
-    std::vector<int> ub(1, 0);
-    const long per_unit = std::max<long>(1, e_off[count] / (4L * num_sms() * 32));
-    long acc = 0;
-    for (int q = 0; q < b->nslices; q++) {
-        acc += sp[q + 1] - sp[q];
-        if (acc >= per_unit || q == b->nslices - 1) {
-            ub.push_back(q + 1);
-            acc = 0;
-        }
-    }
-    b->nunits = (int)ub.size() - 1;
-    FL_TRY(b->unit_slice.alloc(ub.size(), s));
+    // work units over the stacked slices, about four per resident warp
+    std::vector<int> ustep, uslice;
+    b->split = make_units(sp, e_off[count] / (4L * num_sms() * 32), ustep, uslice);
+    b->nunits = (int)uslice.size();
+    FL_TRY(b->unit_step.alloc(ustep.size(), s));
+    FL_TRY(b->unit_slice.alloc(std::max<size_t>(uslice.size(), 1), s));
     FL_TRY(b->perm.alloc(perm.size(), s));
     FL_CUDA(cudaMemcpyAsync(b->slice_ptr.get(), sp.data(), sp.size() * sizeof(int), cudaMemcpyHostToDevice, s));
-    FL_CUDA(cudaMemcpyAsync(b->unit_slice.get(), ub.data(), ub.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+    FL_CUDA(cudaMemcpyAsync(b->unit_step.get(), ustep.data(), ustep.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+    if (!uslice.empty())
+        FL_CUDA(cudaMemcpyAsync(b->unit_slice.get(), uslice.data(), uslice.size() * sizeof(int),
+                                cudaMemcpyHostToDevice, s));
     FL_CUDA(cudaMemcpyAsync(b->perm.get(), perm.data(), perm.size() * sizeof(int), cudaMemcpyHostToDevice, s));
     FL_TRY(b->err.alloc(1, s));
     FL_CUDA(cudaMemsetAsync(b->err.get(), 0, sizeof(int), s));

@@ -97,6 +97,42 @@ static int bits_of(unsigned long v) {
     return b;
 }
 
+bool make_units(const std::vector<int> &sp, long per_unit, std::vector<int> &unit_step,
+                std::vector<int> &unit_slice) {
+    unit_step.clear();
+    unit_slice.clear();
+    const int ns = (int)sp.size() - 1;
+    per_unit = std::max(per_unit, 32L);
+    bool split = false, open = false;
+    long acc = 0;
+    for (int q = 0; q < ns; q++) {
+        const int a = sp[q] >> 5, b = sp[q + 1] >> 5;
+        const long entries = (long)sp[q + 1] - sp[q];
+        if (entries > 2 * per_unit) {
+            // a long slice: pieces of about per_unit entries
+            open = false;
+            const long pieces = (entries + per_unit - 1) / per_unit;
+            const int steps = (int)((b - a + pieces - 1) / pieces);
+            for (int t = a; t < b; t += steps) {
+                unit_step.push_back(t);
+                unit_slice.push_back(q);
+            }
+            split = true;
+            continue;
+        }
+        if (!open) {
+            unit_step.push_back(a);
+            unit_slice.push_back(q);
+            open = true;
+            acc = 0;
+        }
+        acc += entries;
+        if (acc >= per_unit) open = false;
+    }
+    unit_step.push_back(ns > 0 ? sp[ns] >> 5 : 0);
+    return split;
+}
+
 int bucket_auto_band(const int *sortnnz, int n, int nnz, cudaStream_t s, int x_bytes) {
     if (n <= 0 || nnz <= 0) return 0;
     // 16,384 columns of FP64 x, 32,768 of FP32 x: what fits 128 KB of shared
@@ -181,26 +217,21 @@ int build_bucket(Bucket &B, int m, int n, int nnz, const int *sortnnz, const int
     else FL_TRY(H.col32.alloc(std::max(total, 1), s));
     FL_TRY(H.row.alloc(32L * H.nslices, s));
     FL_TRY(H.len.alloc(32L * H.nslices, s));
-    // work units: runs of consecutive slices, sized so the units number
-    // about four per resident warp (never less than one slice) -- enough
-    // units to balance, few enough that the work counter stays cold
+    // work units: about four per resident warp, so that every warp has work
+    // however the nonzeros fall into slices (short, fat matrices have few
+    // slices of great width, and those are cut)
     {
-        std::vector<int> sp(H.nslices + 1);
+        std::vector<int> sp(H.nslices + 1), ustep, uslice;
         FL_TRY(read_ints(s, H.slice_ptr.get(), sp.data(), H.nslices + 1));
-        std::vector<int> ub(1, 0);
-        const long target_units = 4L * num_sms() * 32;
-        const long per_unit = std::max<long>(1, (long)sp[H.nslices] / target_units);
-        long acc = 0;
-        for (int q = 0; q < H.nslices; q++) {
-            acc += sp[q + 1] - sp[q];
-            if (acc >= per_unit || q == H.nslices - 1) {
-                ub.push_back(q + 1);
-                acc = 0;
-            }
-        }
-        H.nunits = (int)ub.size() - 1;
-        FL_TRY(H.unit_slice.alloc(ub.size(), s));
-        FL_CUDA(cudaMemcpyAsync(H.unit_slice.get(), ub.data(), ub.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+        const long per_unit = (long)sp[H.nslices] / (4L * num_sms() * 32);
+        H.split = make_units(sp, per_unit, ustep, uslice);
+        H.nunits = (int)uslice.size();
+        FL_TRY(H.unit_step.alloc(ustep.size(), s));
+        FL_TRY(H.unit_slice.alloc(std::max<size_t>(uslice.size(), 1), s));
+        FL_CUDA(cudaMemcpyAsync(H.unit_step.get(), ustep.data(), ustep.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+        if (!uslice.empty())
+            FL_CUDA(cudaMemcpyAsync(H.unit_slice.get(), uslice.data(), uslice.size() * sizeof(int),
+                                    cudaMemcpyHostToDevice, s));
         FL_CUDA(cudaStreamSynchronize(s));
     }
     k_slice_fill<<<grid_cap(32L * H.nslices, 256, 16), 256, 0, s>>>(
@@ -231,6 +262,7 @@ int spmv_bucket_f64(const Bucket &B, const double *xs, double *y, cudaStream_t s
     a.nslices = H.nnz > 0 ? H.nslices : 0;
     a.nunits = H.nnz > 0 ? H.nunits : 0;
     a.unit_slice = H.unit_slice.get();
+    a.unit_step = H.unit_step.get();
     a.slice_ptr = H.slice_ptr.get();
     a.hrow = H.row.get();
     a.hlen = H.len.get();

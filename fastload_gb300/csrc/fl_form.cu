@@ -147,6 +147,7 @@ static FormArgs<V, Y> form_args(Form &F, const V *lval, const V *hval, const voi
     a.nslices = H.nnz > 0 ? H.nslices : 0;
     a.nunits = H.nnz > 0 ? H.nunits : 0;
     a.unit_slice = H.unit_slice.get();
+    a.unit_step = H.unit_step.get();
     a.slice_ptr = H.slice_ptr.get();
     a.hrow = H.row.get();
     a.hlen = H.len.get();
@@ -169,11 +170,11 @@ int spmv_form(Form &F, int k, const void *xs, void *y, int accumulate, cudaStrea
     const size_t xsz = F.vtype == FL_VALUES_F64 ? sizeof(double) : sizeof(float);
     if (k > 1 && (((uintptr_t)xs % 16) || ((uintptr_t)y % 16)))
         return fail(FL_ERR_ARG, "spmv_form: x and y must be 16-byte aligned for k > 1");
-    // the heavy band owns whole rows when there is no light part: then y is
-    // updated without atomics, and written without zeroing first when every
-    // row has band nonzeros
+    // the heavy band owns whole rows when there is no light part and no
+    // slice is cut across work units: then y is updated without atomics, and
+    // written without zeroing first when every row has band nonzeros
     const bool light = B.light.regions.nitems > 0;
-    const int mode = light ? 0 : (!accumulate && B.heavy.nrows == m ? 2 : 1);
+    const int mode = (light || B.heavy.split) ? 0 : (!accumulate && B.heavy.nrows == m ? 2 : 1);
     if (!accumulate && m && mode != 2) FL_CUDA(cudaMemsetAsync(y, 0, (size_t)m * k * ysz, s));
     if (!light && B.heavy.nnz == 0) return FL_SUCCESS;
     const HeavyBand &H = B.heavy;

@@ -39,7 +39,7 @@ struct FormArgs {
     // heavy band
     int H0, nh, nslices, nunits, bulk;
     int heavy_mode;  // 0: atomic add, 1: y += (rows owned by one lane), 2: y = (every row owned, y not zeroed)
-    const int *slice_ptr, *hrow, *hlen, *unit_slice;
+    const int *slice_ptr, *hrow, *hlen, *unit_slice, *unit_step;
     const V *hval;
     const uint16_t *hcol16;
     const int *hcol32;
@@ -119,81 +119,6 @@ __device__ __forceinline__ void heavy_load_group(const FormArgs<V, Y> &a, int ba
     }
 }
 
-template <typename V, int K, bool XS, bool C16, typename Y>
-__device__ __forceinline__ void heavy_unit(const FormArgs<V, Y> &a, int ub, int ue, const typename VT<V>::X *xsrc,
-                                           int lane) {
-    using A = typename VT<V>::A;
-    using X = typename VT<V>::X;
-    constexpr int G = K == 1 ? (sizeof(A) == 8 ? 4 : 8) : (sizeof(A) == 8 ? 1 : 2);
-    if (ub >= ue) return;
-    int sl = ub;
-    int base = __ldg(a.slice_ptr + sl);
-    int w = (__ldg(a.slice_ptr + sl + 1) - base) >> 5;
-    int r = __ldg(a.hrow + 32 * sl + lane), len = __ldg(a.hlen + 32 * sl + lane);
-    int j0 = 0;
-    A v[G];
-    int c[G];
-    heavy_load_group<V, G, C16, Y>(a, base, j0, len, lane, v, c);
-    A acc[K];
-#pragma unroll
-    for (int q = 0; q < K; q++) acc[q] = (A)0;
-    for (;;) {
-        int nsl = sl, nj0 = j0 + G, nbase = base, nw = w, nr = r, nlen = len;
-        if (nj0 >= w) {
-            nsl = sl + 1;
-            nj0 = 0;
-            if (nsl < ue) {
-                nbase = __ldg(a.slice_ptr + nsl);
-                nw = (__ldg(a.slice_ptr + nsl + 1) - nbase) >> 5;
-                nr = __ldg(a.hrow + 32 * nsl + lane);
-                nlen = __ldg(a.hlen + 32 * nsl + lane);
-            }
-        }
-        const bool has_next = nsl < ue;
-        A nv[G];
-        int nc[G];
-        if (has_next) heavy_load_group<V, G, C16, Y>(a, nbase, nj0, nlen, lane, nv, nc);
-#pragma unroll
-        for (int g = 0; g < G; g++) {
-            if (j0 + g < len) {
-                X xv[K];
-                load_xk<X, K, XS>(xsrc + (size_t)c[g] * K, xv);
-#pragma unroll
-                for (int q = 0; q < K; q++) acc[q] = fma(v[g], (A)xv[q], acc[q]);
-            }
-        }
-        if (nsl != sl) {
-            if (len > 0) {
-                Y *yr = a.y + (size_t)r * K;
-                if (a.heavy_mode == 0) {
-#pragma unroll
-                    for (int q = 0; q < K; q++) atomicAdd(yr + q, (Y)acc[q]);
-                } else if (a.heavy_mode == 1) {
-#pragma unroll
-                    for (int q = 0; q < K; q++) yr[q] += (Y)acc[q];
-                } else {
-#pragma unroll
-                    for (int q = 0; q < K; q++) yr[q] = (Y)acc[q];
-                }
-            }
-#pragma unroll
-            for (int q = 0; q < K; q++) acc[q] = (A)0;
-        }
-        if (!has_next) break;
-        sl = nsl;
-        j0 = nj0;
-        base = nbase;
-        w = nw;
-        r = nr;
-        len = nlen;
-#pragma unroll
-        for (int g = 0; g < G; g++) {
-            v[g] = nv[g];
-            c[g] = nc[g];
-        }
-    }
-}
-
 // y[r] update of a finished row (atomic, read-modify-write or store).
 template <typename A, int K, typename Y>
 __device__ __forceinline__ void heavy_flush(int mode, Y *y, int r, const A acc[K]) {
@@ -209,6 +134,101 @@ __device__ __forceinline__ void heavy_flush(int mode, Y *y, int r, const A acc[K
         for (int q = 0; q < K; q++) yr[q] = (Y)acc[q];
     }
 }
+
+// Heavy unit [T0, T1) (steps), starting in slice sl: lane l owns row l of
+// each slice it reaches and keeps K sums in A.  Software-pipelined over
+// (slice, group of G steps): the next group's value/column loads are issued
+// before the current group's x gathers and FMAs, so each warp keeps two
+// groups of loads in flight; the next slice's metadata is fetched one slice
+// ahead.  A unit may begin or end inside a slice (long slices are cut into
+// several units); each slice part is flushed to y on its own.
+template <typename V, int K, bool XS, bool C16, typename Y>
+__device__ __forceinline__ void heavy_unit(const FormArgs<V, Y> &a, int sl, int T0, int T1,
+                                           const typename VT<V>::X *xsrc, int lane) {
+    using A = typename VT<V>::A;
+    using X = typename VT<V>::X;
+    constexpr int G = K == 1 ? (sizeof(A) == 8 ? 4 : 8) : (sizeof(A) == 8 ? 1 : 2);
+    if (T0 >= T1) return;
+    int base = __ldg(a.slice_ptr + sl);
+    int w = (__ldg(a.slice_ptr + sl + 1) - base) >> 5;
+    int s0 = base >> 5;              // global step of the slice's first entry row
+    int je = min(w, T1 - s0);        // end of this unit's part of the slice
+    int r = __ldg(a.hrow + 32 * sl + lane), len = __ldg(a.hlen + 32 * sl + lane);
+    int lim = min(len, je);
+    int j0 = T0 - s0, jb = j0;       // current step, first step of the part
+    // metadata of slice sl+1 when the unit reaches it
+    int mb = 0, mw = 0, mr = 0, mlen = 0;
+    if (s0 + w < T1) {
+        mb = __ldg(a.slice_ptr + sl + 1);
+        mw = (__ldg(a.slice_ptr + sl + 2) - mb) >> 5;
+        mr = __ldg(a.hrow + 32 * (sl + 1) + lane);
+        mlen = __ldg(a.hlen + 32 * (sl + 1) + lane);
+    }
+    A v[G];
+    int c[G];
+    heavy_load_group<V, G, C16, Y>(a, base, j0, lim, lane, v, c);
+    A acc[K];
+#pragma unroll
+    for (int q = 0; q < K; q++) acc[q] = (A)0;
+    for (;;) {
+        int nsl = sl, nj0 = j0 + G, nbase = base, nw = w, ns0 = s0, nje = je, nr = r, nlen = len, nlim = lim;
+        bool has_next = true;
+        if (nj0 >= je) {
+            has_next = s0 + w < T1;
+            nsl = sl + 1;
+            nj0 = 0;
+            if (has_next) {
+                nbase = mb;
+                nw = mw;
+                nr = mr;
+                nlen = mlen;
+                ns0 = nbase >> 5;
+                nje = min(nw, T1 - ns0);
+                nlim = min(nlen, nje);
+                if (ns0 + nw < T1) {
+                    mb = __ldg(a.slice_ptr + nsl + 1);
+                    mw = (__ldg(a.slice_ptr + nsl + 2) - mb) >> 5;
+                    mr = __ldg(a.hrow + 32 * (nsl + 1) + lane);
+                    mlen = __ldg(a.hlen + 32 * (nsl + 1) + lane);
+                }
+            }
+        }
+        A nv[G];
+        int nc[G];
+        if (has_next) heavy_load_group<V, G, C16, Y>(a, nbase, nj0, nlim, lane, nv, nc);
+#pragma unroll
+        for (int g = 0; g < G; g++) {
+            if (j0 + g < lim) {
+                X xv[K];
+                load_xk<X, K, XS>(xsrc + (size_t)c[g] * K, xv);
+#pragma unroll
+                for (int q = 0; q < K; q++) acc[q] = fma(v[g], (A)xv[q], acc[q]);
+            }
+        }
+        if (nsl != sl) {
+            if (lim > jb) heavy_flush<A, K, Y>(a.heavy_mode, a.y, r, acc);
+#pragma unroll
+            for (int q = 0; q < K; q++) acc[q] = (A)0;
+            jb = 0;
+        }
+        if (!has_next) break;
+        sl = nsl;
+        j0 = nj0;
+        base = nbase;
+        w = nw;
+        s0 = ns0;
+        je = nje;
+        r = nr;
+        len = nlen;
+        lim = nlim;
+#pragma unroll
+        for (int g = 0; g < G; g++) {
+            v[g] = nv[g];
+            c[g] = nc[g];
+        }
+    }
+}
+
 
 // ---- heavy band through a shared-memory ring (K = 1, x and columns narrow) --
 // A unit's slices are contiguous, so its values and 16-bit columns are one
@@ -261,24 +281,25 @@ __device__ __forceinline__ void ring_issue(unsigned char *ring, const V *hval, c
 }
 
 template <typename V, typename Y>
-__device__ __forceinline__ void heavy_unit_ring(const FormArgs<V, Y> &a, int ub, int ue,
+__device__ __forceinline__ void heavy_unit_ring(const FormArgs<V, Y> &a, int sl, int T0, int T1,
                                                 const typename VT<V>::X *xsrc, unsigned char *ring, int lane) {
     using A = typename VT<V>::A;
-    if (ub >= ue) return;
-    const int E0 = __ldg(a.slice_ptr + ub);
-    const int T = (__ldg(a.slice_ptr + ue) - E0) >> 5;
+    if (T0 >= T1) return;
+    const int E0 = 32 * T0;  // first entry of the unit
+    const int T = T1 - T0;   // its steps
     const int nst = (T + RING_STEPS - 1) / RING_STEPS;
 #pragma unroll
     for (int k = 0; k < RING_STAGES; k++) ring_issue<V>(ring, a.hval, a.hcol16, E0, T, k, lane);
-    int bnd = (__ldg(a.slice_ptr + ub + 1) - E0) >> 5;  // first step of the next slice
-    int len = __ldg(a.hlen + 32 * ub + lane), r = __ldg(a.hrow + 32 * ub + lane);
-    int nbnd = T, nlen = 0, nr = 0;
-    if (ub + 1 < ue) {
-        nbnd = (__ldg(a.slice_ptr + ub + 2) - E0) >> 5;
-        nlen = __ldg(a.hlen + 32 * (ub + 1) + lane);
-        nr = __ldg(a.hrow + 32 * (ub + 1) + lane);
+    const int base = __ldg(a.slice_ptr + sl);
+    int bnd = (__ldg(a.slice_ptr + sl + 1) >> 5) - T0;  // unit step where the slice ends
+    int len = __ldg(a.hlen + 32 * sl + lane), r = __ldg(a.hrow + 32 * sl + lane);
+    int j = T0 - (base >> 5), jb = j;                  // step within the slice, first of this part
+    int nbnd = T, nlen = 0, nr = 0;                    // slice sl+1, when the unit reaches it
+    if (bnd < T) {
+        nbnd = (__ldg(a.slice_ptr + sl + 2) >> 5) - T0;
+        nlen = __ldg(a.hlen + 32 * (sl + 1) + lane);
+        nr = __ldg(a.hrow + 32 * (sl + 1) + lane);
     }
-    int sl = ub, j = 0;
     A acc[1] = {(A)0};
     for (int k = 0; k < nst; k++) {
         cp_async_wait<RING_STAGES - 1>();
@@ -295,18 +316,22 @@ __device__ __forceinline__ void heavy_unit_ring(const FormArgs<V, Y> &a, int ub,
                     acc[0] = fma(v, (A)xsrc[sc[32 * q + lane]], acc[0]);
                 }
                 j++;
-                if (t + 1 == bnd) {
-                    if (len > 0) heavy_flush<A, 1, Y>(a.heavy_mode, a.y, r, acc);
+                const bool slice_end = t + 1 == bnd;
+                if (slice_end || t + 1 == T) {
+                    if (len > jb) heavy_flush<A, 1, Y>(a.heavy_mode, a.y, r, acc);
                     acc[0] = (A)0;
-                    sl++;
-                    j = 0;
-                    len = nlen;
-                    r = nr;
-                    bnd = nbnd;
-                    if (sl + 1 < ue) {
-                        nbnd = (__ldg(a.slice_ptr + sl + 2) - E0) >> 5;
-                        nlen = __ldg(a.hlen + 32 * (sl + 1) + lane);
-                        nr = __ldg(a.hrow + 32 * (sl + 1) + lane);
+                    if (slice_end) {
+                        sl++;
+                        j = 0;
+                        jb = 0;
+                        len = nlen;
+                        r = nr;
+                        bnd = nbnd;
+                        if (bnd < T) {
+                            nbnd = (__ldg(a.slice_ptr + sl + 2) >> 5) - T0;
+                            nlen = __ldg(a.hlen + 32 * (sl + 1) + lane);
+                            nr = __ldg(a.hrow + 32 * (sl + 1) + lane);
+                        }
                     }
                 }
             }
@@ -396,12 +421,13 @@ __global__ void __launch_bounds__(FM_THREADS, 1) k_spmv_form(const FormArgs<V, Y
             }
             staged = true;
         }
-        const int ub = __ldg(a.unit_slice + (u - a.nitems)), ue = __ldg(a.unit_slice + (u - a.nitems) + 1);
+        const int ui = u - a.nitems;
+        const int sl = __ldg(a.unit_slice + ui), T0 = __ldg(a.unit_step + ui), T1 = __ldg(a.unit_step + ui + 1);
         if constexpr (RING) {
             const size_t xb = ((size_t)a.nh * K * sizeof(X) + 127) & ~(size_t)127;
-            heavy_unit_ring<V, Y>(a, ub, ue, xsrc, fm_smem + xb + (size_t)(tid >> 5) * ring_warp_bytes<V>(), lane);
+            heavy_unit_ring<V, Y>(a, sl, T0, T1, xsrc, fm_smem + xb + (size_t)(tid >> 5) * ring_warp_bytes<V>(), lane);
         } else {
-            heavy_unit<V, K, XS, C16, Y>(a, ub, ue, xsrc, lane);
+            heavy_unit<V, K, XS, C16, Y>(a, sl, T0, T1, xsrc, lane);
         }
     }
     if (XS && use_band && a.bulk && !staged) {

@@ -7,6 +7,7 @@
 #include <cuda_bf16.h>
 #include <stdint.h>
 #include <string>
+#include <vector>
 
 #include "../../include/fastload.h"
 
@@ -139,9 +140,21 @@ struct HeavyBand {
     DevBuf<int> slice_ptr;      // nslices+1
     DevBuf<int> row;            // 32*nslices, -1 for an empty lane
     DevBuf<int> len;            // 32*nslices
-    int nunits = 0;             // work units: runs of consecutive slices
-    DevBuf<int> unit_slice;     //   (nunits+1 bounds)
+    // Work units are ranges of 32-entry steps (step t = entries 32t..32t+31;
+    // the slices are contiguous, so a range may run over several short
+    // slices or cover part of a long one).
+    int nunits = 0;
+    DevBuf<int> unit_step;      // nunits+1 step bounds
+    DevBuf<int> unit_slice;     // nunits: the slice holding each unit's first step
+    bool split = false;         // a slice is cut across units: its rows' sums meet in y by atomics
 };
+
+// Work units over slices whose entry offsets are sp (nslices+1, multiples
+// of 32): consecutive short slices grouped to about per_unit entries,
+// slices longer than twice that cut into pieces of about per_unit entries.
+// Returns true when a slice was cut.
+bool make_units(const std::vector<int> &sp, long per_unit, std::vector<int> &unit_step,
+                std::vector<int> &unit_slice);
 
 // Bucketed form: light columns [0, H0) keep the FastLoad tile stream, the
 // heavy band [H0, n) uses row slices.
