@@ -374,16 +374,31 @@ static int plan_from_csc(fl_plan_t *out, int m, int n, int nnz, const int *colpt
     p->has_ref = o.with_reference_arrays != 0;
     if (o.heavy_band >= 0) {
         int nh = o.heavy_band;
+        bool wide = false;
         if (nh == 0) {
             nh = bucket_auto_band(p->L.sortnnz.get(), n, nnz, s);
             if (nh < 0) return nh;
+            if (nh == 0 && nnz > 0) {
+                // No dense columns.  Rows as slices (every column in the band,
+                // x through the cache, one y update per row part) beat the
+                // FastLoad stream's atomic per nonzero when x gathers have
+                // locality (banded, block, stencil: mean |r/m - c/n| small)
+                // or when rows are skewed (hot rows make the stream's atomics
+                // collide; cut slices spread them over units).
+                float f[24];
+                FL_TRY(fl_plan_features(p.get(), FL_VALUES_F64, f));
+                if (f[21] < 0.05f || f[22] > 2.0f) {
+                    nh = n;
+                    wide = true;
+                }
+            }
         } else if (nh > bucket_max_band() || nh > n) {
             return fail(FL_ERR_ARG, "plan: heavy_band=%d exceeds min(n=%d, %d)", nh, n, bucket_max_band());
         }
         if (nh > 0) {
             p->bucket.reset(new (std::nothrow) Bucket());
             if (!p->bucket) return fail(FL_ERR_ALLOC, "plan: host allocation failed");
-            FL_TRY(build_bucket(*p->bucket, m, n, nnz, p->L.sortnnz.get(), srow.get(), sval.get(), nh, s));
+            FL_TRY(build_bucket(*p->bucket, m, n, nnz, p->L.sortnnz.get(), srow.get(), sval.get(), nh, s, wide));
         }
     }
     cudaError_t e = cudaStreamSynchronize(s);
@@ -501,7 +516,7 @@ int fl_plan_spmv(fl_plan_t p, const double *d_xs, double *d_y, int accumulate, i
     switch (variant) {
         case FL_KERNEL_AUTO:
             if (p->bucket) return spmv_bucket_f64(*p->bucket, d_xs, d_y, s);
-            return spmv_stream_f64(p->L, d_xs, d_y, FL_KERNEL_STREAM2, s);
+            return spmv_stream_f64(p->L, d_xs, d_y, FL_KERNEL_STREAM, s);
         case FL_KERNEL_BUCKET:
             if (!p->bucket) return fail(FL_ERR_ARG, "plan_spmv: the plan has no heavy band");
             return spmv_bucket_f64(*p->bucket, d_xs, d_y, s);

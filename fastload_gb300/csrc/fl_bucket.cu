@@ -102,7 +102,7 @@ bool make_units(const std::vector<int> &sp, long per_unit, std::vector<int> &uni
     unit_step.clear();
     unit_slice.clear();
     const int ns = (int)sp.size() - 1;
-    per_unit = std::max(per_unit, 32L);
+    per_unit = std::max(per_unit, 1024L);  // below ~32 steps a unit costs more to claim than to run
     bool split = false, open = false;
     long acc = 0;
     for (int q = 0; q < ns; q++) {
@@ -272,7 +272,10 @@ int spmv_bucket_f64(const Bucket &B, const double *xs, double *y, cudaStream_t s
     a.xs = xs;
     a.y = y;
     a.err = B.err.get();
-    a.heavy_mode = 0;
+    // rows are owned by one lane when the band holds every column and no
+    // slice is cut: y (zeroed or accumulated by the caller) is then updated
+    // without atomics
+    a.heavy_mode = (R.nitems == 0 && !H.split) ? 1 : 0;
     const size_t bytes = (size_t)a.nh * sizeof(double);
     a.bulk = a.nh > 0 && ((uintptr_t)(xs + H.H0) % 16 == 0) && bytes % 16 == 0;
     if (a.nitems == 0 && a.nunits == 0) return FL_SUCCESS;

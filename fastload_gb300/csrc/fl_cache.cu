@@ -274,11 +274,12 @@ extern "C" int fl_plan_load(fl_plan_t *out, const char *path, void *stream) {
                                nullptr));
     p->has_ref = h.with_ref != 0;
     if (h.heavy >= 0) {
-        if (h.heavy > bucket_max_band())
-            return fail(FL_ERR_IO, "plan_load: %s: heavy band %d exceeds %d", path, h.heavy, bucket_max_band());
         p->bucket.reset(new (std::nothrow) Bucket());
         if (!p->bucket) return fail(FL_ERR_ALLOC, "plan_load: host allocation failed");
-        FL_TRY(build_bucket(*p->bucket, m, n, nnz, L.sortnnz.get(), srow.get(), sval.get(), h.heavy, s));
+        // bands wider than shared memory hold x (every column, x through the
+        // cache) are rebuilt the way they were built
+        FL_TRY(build_bucket(*p->bucket, m, n, nnz, L.sortnnz.get(), srow.get(), sval.get(), h.heavy, s,
+                            h.heavy > bucket_max_band()));
     }
     srow.release();
     sval.release();

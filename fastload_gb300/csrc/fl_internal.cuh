@@ -150,7 +150,8 @@ struct HeavyBand {
 };
 
 // Work units over slices whose entry offsets are sp (nslices+1, multiples
-// of 32): consecutive short slices grouped to about per_unit entries,
+// of 32): consecutive short slices grouped to about per_unit entries (at
+// least 1,024),
 // slices longer than twice that cut into pieces of about per_unit entries.
 // Returns true when a slice was cut.
 bool make_units(const std::vector<int> &sp, long per_unit, std::vector<int> &unit_step,

@@ -234,10 +234,42 @@ def test_full_size_bucketed(gpu, kind):
             assert p.info["heavy_cols"] == 16384
             assert p.info["heavy_nnz"] > 0.8 * c.nnz
         else:
-            assert p.info["heavy_cols"] == 0  # uniform degrees: no band
+            # no dense columns, but a stencil's x gathers have locality: every
+            # column goes into the band as row slices
+            assert p.info["heavy_cols"] == c.n
         xs = p.permute_x(torch.from_numpy(c.x).cuda())
         ydd = oracle.csc_spmv_dd(c.m, c.n, c.colptr, c.rowidx, c.val, c.x)
         y = p.spmv(xs).cpu().numpy()
         nw, mx = oracle.rel_errors(y, ydd)
         assert nw <= FP64_TOL and mx <= FP64_TOL, (nw, mx)
         p.check()
+
+
+def test_automatic_layout_rule(gpu):
+    """The default plan: a band of dense columns when there are any; with
+    none, row slices over every column when x gathers have locality or rows
+    are skewed, and the plain FastLoad stream for uniformly random rows.
+    Every choice computes the same product."""
+    import torch
+
+    from fastload_gb300 import gen, sweep
+
+    cases = [("random rows", gen.diag_poisson(20000, seed=3), 0),
+             ("stencil", gen.laplacian7(24), "all"),
+             ("skewed rows", sweep._gen_family(4, 20000, 3.0), "all"),
+             ("dense columns", gen.zipf_columns(40000, 1.8, 5000, seed=3), "band")]
+    for name, c, expect in cases:
+        with gpu.Plan.from_csc(c.m, c.n, c.colptr, c.rowidx, c.val) as p:
+            h = p.info["heavy_cols"]
+            if expect == "all":
+                assert h == c.n, (name, h)
+            elif expect == "band":
+                assert 0 < h < c.n, (name, h)
+            else:
+                assert h == 0, (name, h)
+            xs = p.permute_x(torch.from_numpy(c.x).cuda())
+            ydd = oracle.csc_spmv_dd(c.m, c.n, c.colptr, c.rowidx, c.val, c.x)
+            for kern in (gpu.KERNEL_AUTO, gpu.KERNEL_STREAM):
+                y = p.spmv(xs, kernel=kern).cpu().numpy()
+                assert oracle.rel_errors(y, ydd)[0] <= FP64_TOL, (name, kern)
+            p.check()
