@@ -376,22 +376,8 @@ static int plan_from_csc(fl_plan_t *out, int m, int n, int nnz, const int *colpt
         int nh = o.heavy_band;
         bool wide = false;
         if (nh == 0) {
-            nh = bucket_auto_band(p->L.sortnnz.get(), n, nnz, s);
+            nh = auto_layout_band(p->L, 8, &wide, s);
             if (nh < 0) return nh;
-            if (nh == 0 && nnz > 0) {
-                // No dense columns.  Rows as slices (every column in the band,
-                // x through the cache, one y update per row part) beat the
-                // FastLoad stream's atomic per nonzero when x gathers have
-                // locality (banded, block, stencil: mean |r/m - c/n| small)
-                // or when rows are skewed (hot rows make the stream's atomics
-                // collide; cut slices spread them over units).
-                float f[24];
-                FL_TRY(fl_plan_features(p.get(), FL_VALUES_F64, f));
-                if (f[21] < 0.05f || f[22] > 2.0f) {
-                    nh = n;
-                    wide = true;
-                }
-            }
         } else if (nh > bucket_max_band() || nh > n) {
             return fail(FL_ERR_ARG, "plan: heavy_band=%d exceeds min(n=%d, %d)", nh, n, bucket_max_band());
         }

@@ -97,6 +97,27 @@ static int bits_of(unsigned long v) {
     return b;
 }
 
+int auto_layout_band(const Layout &L, int x_bytes, bool *wide, cudaStream_t s) {
+    int nh = bucket_auto_band(L.sortnnz.get(), L.n, L.nnz, s, x_bytes);
+    if (nh < 0) return nh;
+    *wide = nh > bucket_max_band();
+    if (nh == 0 && L.nnz > 0) {
+        // No dense columns.  Rows as slices (every column in the band, x
+        // through the cache, one y update per row part) beat the FastLoad
+        // stream's atomic per nonzero when x gathers have locality (banded,
+        // block, stencil: mean |r/m - c/n| small) or when rows are skewed
+        // (hot rows make the stream's atomics collide; cut slices spread
+        // them over units).
+        float f[24];
+        FL_TRY(plan_features(L, f, s));
+        if (f[21] < 0.05f || f[22] > 2.0f) {
+            nh = L.n;
+            *wide = true;
+        }
+    }
+    return nh;
+}
+
 bool make_units(const std::vector<int> &sp, long per_unit, std::vector<int> &unit_step,
                 std::vector<int> &unit_slice) {
     unit_step.clear();

@@ -110,8 +110,7 @@ int build_form(Form &F, const Layout &L, int vtype, int band, int yf32, cudaStre
         nh = n;
         wide = true;
     } else if (band == FL_BAND_AUTO) {
-        nh = bucket_auto_band(L.sortnnz.get(), n, nnz, s, vtype == FL_VALUES_F64 ? 8 : 4);
-        wide = nh > bucket_max_band();  // FP32 x: up to 32,768 columns of 16-bit indices
+        nh = auto_layout_band(L, vtype == FL_VALUES_F64 ? 8 : 4, &wide, s);
         if (nh < 0) return nh;
     } else if (band > 0) {
         nh = std::min(band, n);

@@ -255,6 +255,13 @@ int bucket_max_band();
 // the densest columns with at least `min_degree` nonzeros, at most the
 // shared-memory limit, or 0 when the band would hold little of the matrix.
 int bucket_auto_band(const int *sortnnz, int n, int nnz, cudaStream_t s, int x_bytes = 8);
+// The 24 tuner features of a layout (host array out[24]; out[23] left 0).
+int plan_features(const Layout &L, float *out, cudaStream_t s);
+// The automatic heavy band of a layout: the densest columns when they hold
+// enough of the matrix; with none, every column as row slices when x
+// gathers have locality or rows are skewed; else no band (0).  *wide is set
+// when the band is wider than shared memory holds x for.
+int auto_layout_band(const Layout &L, int x_bytes, bool *wide, cudaStream_t s);
 
 int num_sms();
 
