@@ -460,16 +460,21 @@ def run_gpu(args, rank, world):
     plan.spmv(xs, y)
     rel = oracle.rel_errors(y.cpu().numpy(), ydd)
 
+    # One step is y = A xs: the library's y-zeroing kernel and the SpMV
+    # kernel, the second launched as a programmatic dependent of the first
+    # (and the next step's zeroing of this step's SpMV), so launches overlap
+    # their start-up.  Events only at the ends of the region: an event
+    # recorded between two launches serialises them.
     def step():
-        y.zero_()
-        plan.spmv(xs, y, accumulate=True, kernel=kernel)
+        plan.spmv(xs, y, kernel=kernel)
 
+    launches_per_step = plan.info["spmv_launches"]
     for _ in range(max(args.warmup, 3)):
         step()
     torch.cuda.synchronize()
     K = args.steps
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    kstart, kend = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
@@ -477,24 +482,31 @@ def run_gpu(args, rank, world):
         wall0 = time.time()
         start.record(stream)
         for i in range(K):
-            y.zero_()
-            ev[i][0].record(stream)
-            plan.spmv(xs, y, accumulate=True, kernel=kernel)
-            ev[i][1].record(stream)
+            step()
         end.record(stream)
         torch.cuda.synchronize()
         wall1 = time.time()
+        # the SpMV kernel alone, K launches back to back accumulating into y:
+        # its average duration for the roofline
+        kstart.record(stream)
+        for i in range(K):
+            plan.spmv(xs, y, accumulate=True, kernel=kernel)
+        kend.record(stream)
+        torch.cuda.synchronize()
+        wall2 = time.time()
     if dist:
         dist.barrier()
     total_ms = start.elapsed_time(end)
-    kern_ms = float(np.mean([a.elapsed_time(b) for a, b in ev]))
+    kern_ms = kstart.elapsed_time(kend) / K
     total_ms = world_max(total_ms, dist, "cuda")
     ms_step = total_ms / K
     peak, peak_kind = measured_peaks()
     value = replica_value(B, world, ms_step)
     achieved = B / (kern_ms * 1e-3) / 1e9
 
-    # the reference-design kernel (one warp per tile) on the same inputs
+    # one launch at a time (the reference-design kernel, the other variants):
+    # a ~50 us device sleep ahead of the start event lets the host enqueue the
+    # launch first, so the events bracket device time, not host launch latency
     def time_kernel(kern, reps=50):
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         for _ in range(3):
@@ -502,6 +514,7 @@ def run_gpu(args, rank, world):
         ts = []
         for _ in range(reps):
             y.zero_()
+            torch.cuda._sleep(100_000)
             a.record(stream)
             plan.spmv(xs, y, accumulate=True, kernel=kern)
             b.record(stream)
@@ -513,6 +526,7 @@ def run_gpu(args, rank, world):
     if plan.info["heavy_cols"]:
         kernels.append(("bucket", fl.KERNEL_BUCKET))
     variants = {} if args.quick else {name: B / (time_kernel(k) * 1e-3) / 1e9 for name, k in kernels}
+    kern_iso_ms = time_kernel(kernel, reps=10 if args.quick else 50)
 
     # end to end through the host-buffer C-ABI call: H2D of x, SpMV, D2H of y
     hx = torch.from_numpy(np.ascontiguousarray(plan.permute_x(x).cpu().numpy())).pin_memory().numpy()
@@ -560,13 +574,17 @@ def run_gpu(args, rank, world):
         "batch": batch,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_kind": f"{peak_kind} hbm_gbs",
-                     "kernel": kname, "bytes_per_launch": B, "kernel_ms": kern_ms},
+                     "kernel": kname, "bytes_per_launch": B, "kernel_ms": kern_ms,
+                     "kernel_ms_isolated": kern_iso_ms,
+                     "timing": "kernel_ms: K back-to-back launches between two events; kernel_ms_isolated: "
+                               "one launch between two events after a device sleep (launch enqueued first), "
+                               "synchronised, L2 not flushed (inputs > L2)"},
         "cpu_baseline": cpu,
         "e2e": {"value": B / e2e_s / 1e9, "unit": "GB/s", "h2d_bytes_per_step": n * 8, "d2h_bytes_per_step": m * 8,
                 "ms_per_step": e2e_s * 1e3, "call": "fl_plan_spmv_host (pinned host x and y)",
                 "rel_err": e2e_rel[0]},
-        "gpu_launches": K,
-        "clocks": clk.summary(wall0, wall1),
+        "gpu_launches": K * launches_per_step,
+        "clocks": clk.summary(wall0, wall2),
     }
     print(json.dumps(line), flush=True)
     plan.close()

@@ -40,6 +40,7 @@ class PlanInfoC(C.Structure):
         ("m", C.c_int), ("n", C.c_int), ("nnz", C.c_int), ("tilenum", C.c_int), ("steps", C.c_int),
         ("segsum", C.c_int), ("regions", C.c_int), ("items", C.c_int), ("device_bytes", C.c_size_t),
         ("heavy_cols", C.c_int), ("heavy_nnz", C.c_int), ("heavy_slices", C.c_int), ("heavy_padded", C.c_int),
+        ("spmv_launches", C.c_int),
     ]
 
 
@@ -65,6 +66,7 @@ SIGNATURES = [
     ("fl_version", C.c_char_p, []),
     ("fl_device_count", C.c_int, []),
     ("fl_debug_fail_alloc_after", None, [C.c_int]),
+    ("fl_debug_hold_x_upload", None, [C.c_int]),
     ("fl_csr_to_csc", C.c_int, [c_double_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
                                 C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("fl_col_sort", C.c_int, [c_double_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,

@@ -6,6 +6,11 @@
 // falls back to a CPU path.
 #include "fl_internal.cuh"
 
+#include <cuda.h>
+
+#include <atomic>
+#include <mutex>
+
 #include <cstdlib>
 #include <cstring>
 #include <memory>
@@ -14,6 +19,33 @@
 namespace fl {
 const char *last_error_cstr();
 void debug_fail_alloc_after(int n);
+// test hook: fl_plan_spmv_host leaves out the epoch copy that releases the
+// kernel's light items
+static std::atomic<bool> g_hold_x_flag{false};
+
+// *flag = *epoch_host once the work queued on s before it is done: a stream
+// memory write (cuStreamWriteValue32, from the driver entry point) where the
+// driver offers it -- it needs no copy engine and lands about a microsecond
+// after the copy before it -- else a 4-byte copy from the pinned word.
+typedef CUresult (*write_value32_fn)(CUstream, CUdeviceptr, cuuint32_t, unsigned int);
+static int signal_epoch(cudaStream_t s, int *flag, const int *epoch_host) {
+    static std::once_flag once;
+    static write_value32_fn fn = nullptr;
+    std::call_once(once, [] {
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuStreamWriteValue32", &f, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (write_value32_fn)f;
+        cudaGetLastError();
+    });
+    if (fn && fn((CUstream)s, (CUdeviceptr)(uintptr_t)flag, (cuuint32_t)*epoch_host, CU_STREAM_WRITE_VALUE_DEFAULT) ==
+                  CUDA_SUCCESS)
+        return FL_SUCCESS;
+    FL_CUDA(cudaMemcpyAsync(flag, epoch_host, sizeof(int), cudaMemcpyHostToDevice, s));
+    return FL_SUCCESS;
+}
 }  // namespace fl
 
 using namespace fl;
@@ -207,6 +239,7 @@ int fl_device_count(void) {
     return n;
 }
 void fl_debug_fail_alloc_after(int countdown) { debug_fail_alloc_after(countdown); }
+void fl_debug_hold_x_upload(int hold) { g_hold_x_flag = hold != 0; }
 
 int fl_csr_to_csc(double *time_ms, int m, int n, int nnz, const double *csr_val, const int *csr_row_ptr,
                   const int *csr_col_ind, double *csc_val, int *csc_row_ind, int *csc_col_ptr, int *nnzpercol) {
@@ -460,9 +493,12 @@ int fl_plan_info_get(fl_plan_t p, fl_plan_info *info) {
     info->heavy_nnz = 0;
     info->heavy_slices = 0;
     info->heavy_padded = 0;
+    info->spmv_launches = (L.m > 0) + (L.regions.nitems > 0);
     if (p->bucket) {
         const Bucket &B = *p->bucket;
         const HeavyBand &H = B.heavy;
+        const bool owned = B.light.regions.nitems == 0 && !H.split && H.nrows == L.m;
+        info->spmv_launches = (L.m > 0 && !owned) + (B.light.regions.nitems > 0 || (H.nnz > 0 && H.nunits > 0));
         info->heavy_cols = H.nh;
         info->heavy_nnz = (int)H.nnz;
         info->heavy_slices = H.nslices;
@@ -498,14 +534,14 @@ int fl_plan_permute_x(fl_plan_t p, const double *d_x, double *d_xs, void *stream
 int fl_plan_spmv(fl_plan_t p, const double *d_xs, double *d_y, int accumulate, int variant, void *stream) {
     if (!p || (p->L.n && !d_xs) || (p->L.m && !d_y)) return fail(FL_ERR_ARG, "plan_spmv: NULL argument");
     cudaStream_t s = (cudaStream_t)stream;
-    if (!accumulate && p->L.m) FL_CUDA(cudaMemsetAsync(d_y, 0, (size_t)p->L.m * sizeof(double), s));
+    if (variant == FL_KERNEL_AUTO && p->bucket) variant = FL_KERNEL_BUCKET;
+    if (variant == FL_KERNEL_BUCKET) {
+        if (!p->bucket) return fail(FL_ERR_ARG, "plan_spmv: the plan has no heavy band");
+        return spmv_bucket_f64(*p->bucket, d_xs, d_y, accumulate, s);
+    }
+    if (!accumulate) FL_TRY(zero_device(d_y, (size_t)p->L.m * sizeof(double), s));
     switch (variant) {
-        case FL_KERNEL_AUTO:
-            if (p->bucket) return spmv_bucket_f64(*p->bucket, d_xs, d_y, s);
-            return spmv_stream_f64(p->L, d_xs, d_y, FL_KERNEL_STREAM, s);
-        case FL_KERNEL_BUCKET:
-            if (!p->bucket) return fail(FL_ERR_ARG, "plan_spmv: the plan has no heavy band");
-            return spmv_bucket_f64(*p->bucket, d_xs, d_y, s);
+        case FL_KERNEL_AUTO: return spmv_stream_f64(p->L, d_xs, d_y, FL_KERNEL_STREAM, s);
         case FL_KERNEL_STREAM:
         case FL_KERNEL_STREAM2: return spmv_stream_f64(p->L, d_xs, d_y, variant, s);
         case FL_KERNEL_TILE: return spmv_tile_f64(p->L, d_xs, d_y, s);
@@ -519,11 +555,68 @@ int fl_plan_spmv_host(fl_plan_t p, const double *h_xs, double *h_y, int variant,
     cudaStream_t s = (cudaStream_t)stream;
     if (p->stage_x.n < (size_t)p->L.n) FL_TRY(p->stage_x.alloc(p->L.n, s));
     if (p->stage_y.n < (size_t)p->L.m) FL_TRY(p->stage_y.alloc(p->L.m, s));
-    if (p->L.n)
-        FL_CUDA(cudaMemcpyAsync(p->stage_x.get(), h_xs, (size_t)p->L.n * sizeof(double), cudaMemcpyHostToDevice, s));
-    FL_TRY(fl_plan_spmv(p, p->stage_x.get(), p->stage_y.get(), 0, variant, stream));
+    double *dx = p->stage_x.get();
+    const Bucket *B = p->bucket.get();
+    const bool overlap = B && (variant == FL_KERNEL_AUTO || variant == FL_KERNEL_BUCKET) && bucket_overlap_ok(*B);
+    if (!overlap) {
+        if (p->L.n)
+            FL_CUDA(cudaMemcpyAsync(dx, h_xs, (size_t)p->L.n * sizeof(double), cudaMemcpyHostToDevice, s));
+        FL_TRY(fl_plan_spmv(p, dx, p->stage_y.get(), 0, variant, stream));
+    } else {
+        // The heavy band reads x only in [H0, n): upload that (at most 128 KB)
+        // on s and launch.  The light columns' x [0, H0) follows on the side
+        // stream, then the call's epoch into x_flag.  The kernel runs the
+        // band while that copy is in flight and takes the light items once
+        // the epoch is in.
+        const int H0 = B->heavy.H0;
+        if (!p->side) {
+            FL_CUDA(cudaStreamCreateWithFlags(&p->side, cudaStreamNonBlocking));
+            FL_CUDA(cudaEventCreateWithFlags(&p->fork, cudaEventDisableTiming));
+            FL_CUDA(cudaEventCreateWithFlags(&p->join, cudaEventDisableTiming));
+        }
+        if (!p->epoch_host) {
+            // [0] the epoch word, [1] the kernel's status word (written by the
+            // kernel through the mapping only when a wait expires)
+            FL_CUDA(cudaHostAlloc((void **)&p->epoch_host, 2 * sizeof(int), cudaHostAllocMapped));
+            p->epoch_host[0] = p->epoch_host[1] = 0;
+            FL_CUDA(cudaHostGetDevicePointer((void **)&p->epoch_dev, p->epoch_host, 0));
+        }
+        if (!p->x_flag.get()) {
+            FL_TRY(p->x_flag.alloc(1, s));
+            FL_CUDA(cudaMemsetAsync(p->x_flag.get(), 0, sizeof(int), s));
+        }
+        // the previous call has finished (this call is synchronous), so the
+        // pinned words are free to rewrite
+        p->epoch = (int)((unsigned)p->epoch + 1u);  // compared modulo 2^32 by the kernel
+        p->epoch_host[0] = p->epoch;
+        p->epoch_host[1] = 0;
+        // the band's x first: host-to-device copies share a copy engine, so
+        // a band copy queued behind the light columns' would wait for it
+        FL_CUDA(cudaMemcpyAsync(dx + H0, h_xs + H0, (size_t)(p->L.n - H0) * sizeof(double),
+                                cudaMemcpyHostToDevice, s));
+        // the side stream follows earlier work on s that reads stage_x or
+        // x_flag, but not this call's kernel (which waits for it)
+        FL_CUDA(cudaEventRecord(p->fork, s));
+        // launched first, so the host's remaining calls overlap the band
+        const XUpload xu{p->x_flag.get(), p->epoch, p->epoch_dev + 1};
+        FL_TRY(spmv_bucket_f64(*B, dx, p->stage_y.get(), 0, s, &xu));
+        // nothing queued after the kernel is issued before these, so no copy
+        // the kernel waits for sits behind one that waits for the kernel
+        FL_CUDA(cudaStreamWaitEvent(p->side, p->fork, 0));
+        FL_CUDA(cudaMemcpyAsync(dx, h_xs, (size_t)H0 * sizeof(double), cudaMemcpyHostToDevice, p->side));
+        if (!g_hold_x_flag) FL_TRY(signal_epoch(p->side, p->x_flag.get(), p->epoch_host));
+        FL_CUDA(cudaEventRecord(p->join, p->side));
+        FL_CUDA(cudaStreamWaitEvent(s, p->join, 0));
+    }
     FL_TRY(download(h_y, p->stage_y.get(), p->L.m, s));
     FL_CUDA(cudaStreamSynchronize(s));
+    if (overlap && *(volatile int *)(p->epoch_host + 1)) {
+        const int h = p->epoch_host[1];
+        p->epoch_host[1] = 0;
+        FL_CUDA(cudaMemsetAsync(B->err.get(), 0, sizeof(int), s));
+        FL_CUDA(cudaStreamSynchronize(s));
+        return fail(FL_ERR_NOT_READY, "plan_spmv_host: a bounded device wait expired (0x%x); y is incomplete", h);
+    }
     return FL_SUCCESS;
 }
 
@@ -580,7 +673,10 @@ int fl_plan_check(fl_plan_t p) {
         int h = 0;
         FL_CUDA(cudaMemcpy(&h, b->err.get(), sizeof(int), cudaMemcpyDeviceToHost));
         FL_CUDA(cudaMemset(b->err.get(), 0, sizeof(int)));
-        if (h) return fail(FL_ERR_NOT_READY, "staging of the heavy band's x did not complete (0x%x)", h);
+        if (h)
+            return fail(FL_ERR_NOT_READY,
+                        "a bounded device wait expired (0x%x: 1, 2 staging of the heavy band's x; 4 the upload of "
+                        "the light columns' x)", h);
     }
     return FL_SUCCESS;
 }

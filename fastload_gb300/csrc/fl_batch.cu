@@ -96,7 +96,7 @@ size_t vsize(int vtype) { return vtype == FL_VALUES_F64 ? 8 : 4; }
 
 int launch(fl_batch *b, const void *xs, void *y, cudaStream_t s) {
     const size_t ysz = b->yf32 ? sizeof(float) : sizeof(double);
-    if (b->M && (!b->all_rows || b->split)) FL_CUDA(cudaMemsetAsync(y, 0, (size_t)b->M * ysz, s));
+    if (!b->all_rows || b->split) FL_TRY(zero_device(y, (size_t)b->M * ysz, s));
     if (b->nunits == 0) return FL_SUCCESS;
     auto fill = [&](auto &a) {
         a.items = nullptr;
@@ -120,6 +120,9 @@ int launch(fl_batch *b, const void *xs, void *y, cudaStream_t s) {
         a.hcol16 = nullptr;
         a.hcol32 = b->col.get();
         a.err = b->err.get();
+        a.x_ready = nullptr;
+        a.x_epoch = 0;
+        a.err_host = nullptr;
     };
     if (b->vtype == FL_VALUES_F64) {
         FormArgs<double, double> a;

@@ -269,7 +269,16 @@ int build_bucket(Bucket &B, int m, int n, int nnz, const int *sortnnz, const int
 // heavy units with x staged in shared memory by a TMA bulk copy.
 int run_form_f64(const FormArgs<double, double> &a, int k, bool wide, cudaStream_t s);
 
-int spmv_bucket_f64(const Bucket &B, const double *xs, double *y, cudaStream_t s) {
+bool bucket_overlap_ok(const Bucket &B) {
+    const HeavyBand &H = B.heavy;
+    // light and heavy parts, and the band's x staged in shared memory (the
+    // kernels that take the light x late are those)
+    return B.light.regions.nitems > 0 && H.nnz > 0 && H.nunits > 0 && H.H0 > 0 && H.nh > 0 &&
+           (size_t)H.nh * sizeof(double) <= (size_t)FM_SMEM_MAX && H.nh <= 65535;
+}
+
+int spmv_bucket_f64(const Bucket &B, const double *xs, double *y, int accumulate, cudaStream_t s,
+                    const XUpload *xu) {
     const HeavyBand &H = B.heavy;
     const Regions &R = B.light.regions;
     FormArgs<double, double> a;
@@ -293,10 +302,21 @@ int spmv_bucket_f64(const Bucket &B, const double *xs, double *y, cudaStream_t s
     a.xs = xs;
     a.y = y;
     a.err = B.err.get();
+    a.x_ready = nullptr;
+    a.x_epoch = 0;
+    a.err_host = nullptr;
+    if (xu) {
+        if (!bucket_overlap_ok(B)) return fail(FL_ERR_ARG, "spmv_bucket: overlapped upload does not apply");
+        a.x_ready = xu->flag;
+        a.x_epoch = xu->epoch;
+        a.err_host = xu->err_host;
+    }
     // rows are owned by one lane when the band holds every column and no
-    // slice is cut: y (zeroed or accumulated by the caller) is then updated
-    // without atomics
-    a.heavy_mode = (R.nitems == 0 && !H.split) ? 1 : 0;
+    // slice is cut: y is then updated without atomics, and written without
+    // zeroing first when every row has band nonzeros
+    const int m = B.light.m;
+    a.heavy_mode = (R.nitems > 0 || H.split) ? 0 : (!accumulate && H.nrows == m ? 2 : 1);
+    if (!accumulate && a.heavy_mode != 2) FL_TRY(zero_device(y, (size_t)m * sizeof(double), s));
     const size_t bytes = (size_t)a.nh * sizeof(double);
     a.bulk = a.nh > 0 && ((uintptr_t)(xs + H.H0) % 16 == 0) && bytes % 16 == 0;
     if (a.nitems == 0 && a.nunits == 0) return FL_SUCCESS;

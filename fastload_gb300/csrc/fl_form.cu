@@ -156,6 +156,9 @@ static FormArgs<V, Y> form_args(Form &F, const V *lval, const V *hval, const voi
     a.xs = (const typename VT<V>::X *)xs;
     a.y = (Y *)y;
     a.err = B.err.get();
+    a.x_ready = nullptr;
+    a.x_epoch = 0;
+    a.err_host = nullptr;
     a.heavy_mode = 0;
     a.bulk = 0;
     return a;
@@ -174,7 +177,7 @@ int spmv_form(Form &F, int k, const void *xs, void *y, int accumulate, cudaStrea
     // written without zeroing first when every row has band nonzeros
     const bool light = B.light.regions.nitems > 0;
     const int mode = (light || B.heavy.split) ? 0 : (!accumulate && B.heavy.nrows == m ? 2 : 1);
-    if (!accumulate && m && mode != 2) FL_CUDA(cudaMemsetAsync(y, 0, (size_t)m * k * ysz, s));
+    if (!accumulate && mode != 2) FL_TRY(zero_device(y, (size_t)m * k * ysz, s));
     if (!light && B.heavy.nnz == 0) return FL_SUCCESS;
     const HeavyBand &H = B.heavy;
     const size_t band_bytes = (size_t)H.nh * k * xsz;

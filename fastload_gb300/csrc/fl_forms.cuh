@@ -20,11 +20,14 @@
 #include "fl_stream.cuh"
 
 #include <algorithm>
+#include <mutex>
+#include <type_traits>
 
 namespace fl {
 
 constexpr int FM_THREADS = 1024;
 constexpr long FM_WAIT_LIMIT = 1L << 20;
+constexpr long FM_FLAG_LIMIT = 1L << 20;  // polls of x_ready (an L2 round trip and a short sleep each): about a second
 constexpr int FM_SMEM_MAX = 196608;  // dynamic shared memory budget of the form kernels
 
 template <typename V, typename Y>
@@ -46,7 +49,23 @@ struct FormArgs {
     const X *xs;
     Y *y;
     int *err;
+    // x of the light columns still in flight (host call with overlapped
+    // upload, kernels instantiated with OVL): it is in once *x_ready reaches
+    // x_epoch.  nullptr: x complete at launch.
+    const int *x_ready;
+    int x_epoch;
+    // host-mapped status word of a synchronous host call (nullptr: none):
+    // an expired wait is also reported there, so the call needs no readback
+    int *err_host;
 };
+
+// An expired bounded wait: bits into the launch's status word (and the host
+// call's mapped word).
+template <typename V, typename Y>
+__device__ __forceinline__ void form_fail(const FormArgs<V, Y> &a, int bits) {
+    atomicOr(a.err, bits);
+    if (a.err_host) *(volatile int *)a.err_host = bits;
+}
 
 // K > 1 light item: K lanes per nonzero, lane (g, r) adds the rhs-r product
 // of nonzero e+g; a warp instruction's atomics cover 32/K rows x K
@@ -343,16 +362,45 @@ __device__ __forceinline__ void heavy_unit_ring(const FormArgs<V, Y> &a, int sl,
     __syncwarp();
 }
 
-template <typename V, int K, bool XS, bool C16, typename Y, bool RING = false>
+// Whether the light columns' x is in (acquire: its bytes are visible to
+// the reading thread afterwards).
+template <typename V, typename Y>
+__device__ __forceinline__ bool light_x_in(const FormArgs<V, Y> &a) {
+    int v;
+    asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(a.x_ready) : "memory");
+    return (int)((unsigned)v - (unsigned)a.x_epoch) >= 0;
+}
+
+// Block-shared word: some warp of the block has acquired the light x.
+// Published with release, read with acquire, so a warp reading it inherits
+// the acquiring warp's view of x.
+__device__ __forceinline__ int shared_acquire(const int *w) {
+    int v;
+    asm volatile("ld.acquire.cta.shared::cta.b32 %0, [%1];" : "=r"(v) : "r"((uint32_t)__cvta_generic_to_shared(w))
+                 : "memory");
+    return v;
+}
+__device__ __forceinline__ void shared_release(int *w, int v) {
+    asm volatile("st.release.cta.shared::cta.b32 [%0], %1;" ::"r"((uint32_t)__cvta_generic_to_shared(w)), "r"(v)
+                 : "memory");
+}
+
+template <typename V, int K, bool XS, bool C16, typename Y, bool RING = false, bool OVL = false>
 __global__ void __launch_bounds__(FM_THREADS, 1) k_spmv_form(const FormArgs<V, Y> a) {
     using X = typename VT<V>::X;
     extern __shared__ __align__(128) unsigned char fm_smem[];
     X *xh = (X *)fm_smem;
     __shared__ __align__(8) unsigned long long mbar;
-    __shared__ int claimed;  // units of this block handed out so far
+    __shared__ int claimed;    // units (OVL: light items) of this block handed out so far
+    __shared__ int claimed_h;  // OVL: heavy units handed out
+    __shared__ int x_in;       // OVL: some warp of the block has acquired the light x
     const int tid = threadIdx.x, lane = tid & 31;
     const uint32_t bar = (uint32_t)__cvta_generic_to_shared(&mbar);
-    if (tid == 0) claimed = 0;
+    if (tid == 0) claimed = claimed_h = x_in = 0;
+    // Launched as a programmatic dependent of the kernel before it (the y
+    // zeroing): the block may be resident before that kernel ends, so wait
+    // for it before reading or writing anything.
+    asm volatile("griddepcontrol.wait;" ::: "memory");
     const bool use_band = a.nh > 0 && a.nslices > 0;
     if (XS && use_band) {
         const uint32_t bytes = (uint32_t)a.nh * K * (uint32_t)sizeof(X);
@@ -390,19 +438,10 @@ __global__ void __launch_bounds__(FM_THREADS, 1) k_spmv_form(const FormArgs<V, Y
     // kinds; inside the block warps claim the block's units through a
     // shared-memory counter.  No global atomics, no per-launch reset.
     __syncthreads();
-    const int G = gridDim.x;
-    const int mine = total > (int)blockIdx.x ? (total - 1 - (int)blockIdx.x) / G + 1 : 0;
-    for (;;) {
-        int k = 0;
-        if (lane == 0) k = atomicAdd(&claimed, 1);
-        k = __shfl_sync(FULLM, k, 0);
-        if (k >= mine) break;
-        const int u = (int)blockIdx.x + G * k;
-        if (u < a.nitems) {
-            if constexpr (K == 1) stream_item<V, Y, 1>(a.items[u], a.regions, a.row, a.val, a.xs, a.y, lane);
-            else light_item_kn<V, K, Y>(a.items[u], a.regions, a.row, a.val, a.xs, a.y, lane);
-            continue;
-        }
+    const int G = gridDim.x, b = (int)blockIdx.x;
+    const int mine = total > b ? (total - 1 - b) / G + 1 : 0;
+    // one heavy unit; the first waits (bounded) for the band's staged x
+    auto heavy = [&](int ui) -> bool {
         if (!staged) {
             bool ok = false;
             for (long i = 0; i < FM_WAIT_LIMIT && !ok; i++) {
@@ -416,18 +455,114 @@ __global__ void __launch_bounds__(FM_THREADS, 1) k_spmv_form(const FormArgs<V, Y
                 ok = done != 0;
             }
             if (!ok) {
-                if (lane == 0) atomicOr(a.err, 1);
-                break;
+                if (lane == 0) form_fail(a, 1);
+                return false;
             }
             staged = true;
         }
-        const int ui = u - a.nitems;
         const int sl = __ldg(a.unit_slice + ui), T0 = __ldg(a.unit_step + ui), T1 = __ldg(a.unit_step + ui + 1);
         if constexpr (RING) {
             const size_t xb = ((size_t)a.nh * K * sizeof(X) + 127) & ~(size_t)127;
             heavy_unit_ring<V, Y>(a, sl, T0, T1, xsrc, fm_smem + xb + (size_t)(tid >> 5) * ring_warp_bytes<V>(), lane);
         } else {
             heavy_unit<V, K, XS, C16, Y>(a, sl, T0, T1, xsrc, lane);
+        }
+        return true;
+    };
+    auto light = [&](int u) {
+        if constexpr (K == 1) stream_item<V, Y, 1>(a.items[u], a.regions, a.row, a.val, a.xs, a.y, lane);
+        else light_item_kn<V, K, Y>(a.items[u], a.regions, a.row, a.val, a.xs, a.y, lane);
+    };
+    if constexpr (!OVL) {
+        // Work distribution: unit u (light items first, then heavy units)
+        // goes to block u % gridDim.x, so every block gets an even share of
+        // both kinds; inside the block warps claim the block's units through
+        // a shared-memory counter.  No global atomics, no per-launch reset.
+        for (;;) {
+            int k = 0;
+            if (lane == 0) k = atomicAdd(&claimed, 1);
+            k = __shfl_sync(FULLM, k, 0);
+            if (k >= mine) break;
+            const int u = b + G * k;
+            if (u < a.nitems) {
+                light(u);
+                continue;
+            }
+            if (!heavy(u - a.nitems)) break;
+        }
+    } else {
+        // The light columns' x is still arriving.  The block's units are
+        // dealt as above; a warp takes a heavy unit while the x is not in,
+        // then the light items, and waits (bounded) for the x only when no
+        // heavy unit is left.
+        const int ml = a.nitems > b ? (a.nitems - 1 - b) / G + 1 : 0;  // this block's light items
+        const int mh = mine - ml;                                        // and heavy units
+        bool have = false;  // this warp has acquired the light x
+        for (;;) {
+            int kind = 0, k = 0;  // 0 none left, 1 light item k, 2 heavy unit k
+            if (lane == 0) {
+                for (;;) {
+                    const int jl = *(volatile int *)&claimed, jh = *(volatile int *)&claimed_h;
+                    const bool lav = jl < ml, hav = jh < mh;
+                    if (!lav && !hav) break;
+                    bool take_light = !hav;
+                    if (lav && hav) {
+                        take_light = have || *(volatile int *)&x_in;
+                        if (!take_light && light_x_in(a)) {
+                            shared_release(&x_in, 1);
+                            take_light = true;
+                        }
+                    }
+                    if (take_light) {
+                        k = atomicAdd(&claimed, 1);
+                        if (k < ml) {
+                            kind = 1;
+                            break;
+                        }
+                    } else {
+                        k = atomicAdd(&claimed_h, 1);
+                        if (k < mh) {
+                            kind = 2;
+                            break;
+                        }
+                    }
+                }
+            }
+            kind = __shfl_sync(FULLM, kind, 0);
+            k = __shfl_sync(FULLM, k, 0);
+            if (kind == 0) break;
+            if (kind == 2) {
+                if (!heavy(b + G * (ml + k) - a.nitems)) break;
+                continue;
+            }
+            if (!have) {
+                // acquire the light x: through the block's word when another
+                // warp already has, else from the flag (bounded wait)
+                int ok = 0;
+                if (lane == 0) {
+                    for (long i = 0; i < FM_FLAG_LIMIT; i++) {
+                        if (shared_acquire(&x_in)) {
+                            ok = 1;
+                            break;
+                        }
+                        if (light_x_in(a)) {
+                            ok = 1;
+                            shared_release(&x_in, 1);
+                            break;
+                        }
+                        if (*(volatile int *)a.err & 4) break;  // another warp already gave up
+                        __nanosleep(200);
+                    }
+                }
+                ok = __shfl_sync(FULLM, ok, 0);
+                __syncwarp();  // lane 0's acquire orders the warp's x loads
+                if (!ok) {
+                    if (lane == 0) form_fail(a, 4);
+                    break;
+                }
+                have = true;
+            }
+            light(b + G * k);
         }
     }
     if (XS && use_band && a.bulk && !staged) {
@@ -442,22 +577,49 @@ __global__ void __launch_bounds__(FM_THREADS, 1) k_spmv_form(const FormArgs<V, Y
                 : "memory");
             ok = done != 0;
         }
-        if (!ok && lane == 0) atomicOr(a.err, 2);
+        if (!ok && lane == 0) form_fail(a, 2);
     }
+    // this block is done: a dependent launch behind this kernel may start
+    // (it waits for this kernel's completion before touching memory)
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
 
 // Launch of one form kernel; xs/y typed per the form.
-template <typename V, int K, bool XS, bool C16, typename Y, bool RING = false>
+template <typename V, int K, bool XS, bool C16, typename Y, bool RING = false, bool OVL = false>
 int launch_form(const FormArgs<V, Y> &a, size_t smem, cudaStream_t s) {
-    auto kern = k_spmv_form<V, K, XS, C16, Y, RING>;
-    if (smem > 0) FL_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    auto kern = k_spmv_form<V, K, XS, C16, Y, RING, OVL>;
+    // the shared-memory opt-in and the occupancy query cost host time on
+    // every launch: done once per (instantiation, shared-memory size)
+    static std::mutex mu;
+    static size_t smem_opted = 0, occ_smem = ~(size_t)0;
+    static int occ_per_sm = 0;
     int per_sm = 0;
-    FL_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, FM_THREADS, smem));
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        if (smem > smem_opted) {
+            FL_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            smem_opted = smem;
+        }
+        if (smem != occ_smem) {
+            FL_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_per_sm, kern, FM_THREADS, smem));
+            occ_smem = smem;
+        }
+        per_sm = occ_per_sm;
+    }
     if (per_sm <= 0) per_sm = 1;
     const long units = (long)a.nitems + a.nunits;
     const long grid = std::max<long>(1, std::min<long>((long)num_sms() * per_sm, (units + 31) / 32));
-    kern<<<(int)grid, FM_THREADS, smem, s>>>(a);
-    FL_CUDA(cudaGetLastError());
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(FM_THREADS);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    FL_CUDA(cudaLaunchKernelEx(&cfg, kern, a));
     return FL_SUCCESS;
 }
 
@@ -473,8 +635,16 @@ int dispatch_form(const FormArgs<V, Y> &a, int k, bool wide_cols, cudaStream_t s
         // rings fit beside each other
         const size_t xb = (smem + 127) & ~(size_t)127;
         const size_t ring = (size_t)(FM_THREADS / 32) * ring_warp_bytes<V>();
-        if (xs_smem && a.nslices > 0 && xb + ring <= (size_t)SMEM_OPTIN)
-            return launch_form<V, 1, true, true, Y, true>(a, xb + ring, s);
+        const bool use_ring = xs_smem && a.nslices > 0 && xb + ring <= (size_t)SMEM_OPTIN;
+        if (a.x_ready) {
+            // x still arriving (FP64 host call): only the staged-band kernels
+            if constexpr (std::is_same<V, double>::value && std::is_same<Y, double>::value) {
+                if (use_ring) return launch_form<V, 1, true, true, Y, true, true>(a, xb + ring, s);
+                if (xs_smem) return launch_form<V, 1, true, true, Y, false, true>(a, dyn, s);
+            }
+            return fail(FL_ERR_ARG, "spmv_form: overlapped upload needs the band's x in shared memory");
+        }
+        if (use_ring) return launch_form<V, 1, true, true, Y, true>(a, xb + ring, s);
         if (xs_smem) return launch_form<V, 1, true, true, Y>(a, dyn, s);
         if (!wide_cols) return launch_form<V, 1, false, true, Y>(a, 0, s);
         return launch_form<V, 1, false, false, Y>(a, 0, s);

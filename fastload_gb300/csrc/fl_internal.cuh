@@ -243,12 +243,29 @@ int permute_x(const int *perm, int n, const double *x, double *xs, cudaStream_t 
 int spmv_stream_f64(const Layout &L, const double *xs, double *y, int variant,
                     cudaStream_t s);
 int spmv_tile_f64(const Layout &L, const double *xs, double *y, cudaStream_t s);
+// bytes (a multiple of 4) of zeros at p, by a kernel that the SpMV kernel
+// launched behind it on s may overlap (programmatic dependent launch)
+int zero_device(void *p, size_t bytes, cudaStream_t s);
 // Bucketed form: build from the column-sorted CSC (device) and run.
 // wide: allow a band of up to all n columns (x then read from global memory
 // by the form kernels); otherwise the band is capped at bucket_max_band().
 int build_bucket(Bucket &B, int m, int n, int nnz, const int *sortnnz, const int *srow_tmp,
                  const double *sval_tmp, int nh, cudaStream_t s, bool wide = false);
-int spmv_bucket_f64(const Bucket &B, const double *xs, double *y, cudaStream_t s);
+// The light columns' x (xs[0, H0)) still arriving while the bucket kernel
+// runs (the overlapped host call): it is in once *flag reaches epoch;
+// err_host is the device view of a host-mapped word that receives the
+// status bits of an expired wait.
+struct XUpload {
+    const int *flag;
+    int epoch;
+    int *err_host;
+};
+// Whether the overlapped upload applies to B: light and heavy parts, the
+// band's x staged in shared memory.
+bool bucket_overlap_ok(const Bucket &B);
+// y = A xs (accumulate 0) or y += A xs; xu: see XUpload (nullptr: x complete).
+int spmv_bucket_f64(const Bucket &B, const double *xs, double *y, int accumulate, cudaStream_t s,
+                    const XUpload *xu = nullptr);
 // Largest heavy band the bucket kernel can stage in shared memory.
 int bucket_max_band();
 // Heavy band width chosen from the sorted column counts (device array):
@@ -285,4 +302,23 @@ struct fl_plan {
     std::unique_ptr<fl::Bucket> bucket;           // bucketed FP64 form (heavy band), optional
     std::vector<std::unique_ptr<fl::Form>> forms; // storage / rhs forms
     fl::DevBuf<double> stage_x, stage_y;          // device staging of fl_plan_spmv_host
+    // fl_plan_spmv_host overlaps the upload of the light columns' x with the
+    // heavy band: that copy runs on a side stream, followed by a write of the
+    // call's epoch into x_flag, on which the kernel's light items wait
+    // (bounded)
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
+    fl::DevBuf<int> x_flag;
+    int *epoch_host = nullptr;                   // pinned, mapped: [0] epoch, [1] status
+    int *epoch_dev = nullptr;                    // device view of epoch_host
+    int epoch = 0;
+    fl_plan() = default;
+    fl_plan(const fl_plan &) = delete;
+    fl_plan &operator=(const fl_plan &) = delete;
+    ~fl_plan() {
+        if (side) cudaStreamDestroy(side);
+        if (fork) cudaEventDestroy(fork);
+        if (join) cudaEventDestroy(join);
+        if (epoch_host) cudaFreeHost(epoch_host);
+    }
 };

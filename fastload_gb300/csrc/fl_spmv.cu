@@ -18,6 +18,8 @@
 //    FP64 pipe is narrow and would otherwise bound the kernel).
 #include "fl_stream.cuh"
 
+#include <algorithm>
+
 namespace fl {
 
 template <int U>
@@ -100,6 +102,45 @@ int spmv_stream_f64(const Layout &L, const double *xs, double *y, int variant, c
                                                   L.val.get(), xs, y);
     }
     FL_CUDA(cudaGetLastError());
+    return FL_SUCCESS;
+}
+
+// y = 0 ahead of an accumulating SpMV kernel.  Launched as a programmatic
+// dependent of the kernel before it (griddepcontrol): its blocks may be
+// scheduled while that kernel drains, wait for it to finish, then release
+// the SpMV kernel behind them before storing, so the two launches overlap
+// their start-up.  words: 4-byte words; p16: p is 16-byte aligned.
+__global__ void __launch_bounds__(512) k_zero_words(unsigned *p, long words, int p16) {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    const long t = blockIdx.x * (long)blockDim.x + threadIdx.x, T = (long)gridDim.x * blockDim.x;
+    long head = 0;
+    if (p16) {
+        const long n4 = words >> 2;
+        uint4 *q = reinterpret_cast<uint4 *>(p);
+        for (long i = t; i < n4; i += T) q[i] = make_uint4(0u, 0u, 0u, 0u);
+        head = n4 << 2;
+    }
+    for (long i = head + t; i < words; i += T) p[i] = 0u;
+}
+
+int zero_device(void *p, size_t bytes, cudaStream_t s) {
+    if (bytes == 0) return FL_SUCCESS;
+    if (bytes % 4 || (uintptr_t)p % 4) return fail(FL_ERR_ARG, "zero_device: %zu bytes at %p", bytes, p);
+    const long words = (long)(bytes / 4);
+    const int p16 = (uintptr_t)p % 16 == 0;
+    const long per_block = 512L * 16 * 4;  // 16 bytes per thread per pass, about four passes
+    const long grid = std::max<long>(1, std::min<long>((long)num_sms() * 4, ((long)bytes + per_block - 1) / per_block));
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(512);
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    FL_CUDA(cudaLaunchKernelEx(&cfg, k_zero_words, (unsigned *)p, words, p16));
     return FL_SUCCESS;
 }
 

@@ -129,6 +129,9 @@ typedef struct fl_plan_info {
     int heavy_nnz;   /* nonzeros in the heavy band */
     int heavy_slices;/* 32-row slices of the heavy band */
     int heavy_padded;/* slice entries including padding */
+    int spmv_launches; /* kernels one fl_plan_spmv(accumulate 0, FL_KERNEL_AUTO)
+                          launches: the y zeroing (skipped when the band owns
+                          every row) and the SpMV kernel */
 } fl_plan_info;
 
 /* Plan build options (NULL = defaults: no reference arrays, automatic
@@ -443,6 +446,11 @@ int fl_col_sort_noalloc(int n, int nnz, const int *d_nnzpercol,
 /* Makes the `countdown`-th device allocation from now fail with
  * FL_ERR_ALLOC (0 disables).  For error-path tests. */
 void fl_debug_fail_alloc_after(int countdown);
+
+/* hold != 0: fl_plan_spmv_host stops signalling that the light columns' x
+ * has arrived, so the kernel's bounded wait for it runs out (about a second)
+ * and the call returns FL_ERR_NOT_READY.  For the failure-detection test. */
+void fl_debug_hold_x_upload(int hold);
 
 #ifdef __cplusplus
 }

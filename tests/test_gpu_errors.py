@@ -96,3 +96,34 @@ def test_tile_kernel_needs_reference_arrays(gpu):
             p.spmv(xs, kernel=gpu.KERNEL_TILE)
         with pytest.raises(gpu.FastLoadError):
             p.export()
+
+
+def test_host_call_overlapped_upload_and_its_bounded_wait(gpu):
+    """fl_plan_spmv_host uploads the light columns' x on a side stream while
+    the heavy band runs; the light items wait for an epoch word that follows
+    the copy.  Held back (test hook), the wait runs out after about a second,
+    the call reports FL_ERR_NOT_READY, and the next call is correct."""
+    import oracle
+    from fastload_gb300 import _lib, gen
+
+    lib = _lib.load()
+    c = gen.zipf_columns(40000, 1.8, 5000, seed=3)
+    ydd = oracle.csc_spmv_dd(c.m, c.n, c.colptr, c.rowidx, c.val, c.x)
+    with gpu.Plan.from_csc(c.m, c.n, c.colptr, c.rowidx, c.val) as p:
+        assert 0 < p.info["heavy_cols"] < c.n and p.info["items"] > 0
+        import torch
+
+        hx = p.permute_x(torch.from_numpy(c.x).cuda()).cpu().numpy()
+        for _ in range(3):
+            y = p.spmv_host(hx)
+            assert oracle.rel_errors(y, ydd)[0] <= 1e-12
+        lib.fl_debug_hold_x_upload(1)
+        try:
+            with pytest.raises(gpu.FastLoadError) as e:
+                p.spmv_host(hx)
+            assert e.value.code == -6, e.value
+        finally:
+            lib.fl_debug_hold_x_upload(0)
+        y = p.spmv_host(hx)
+        assert oracle.rel_errors(y, ydd)[0] <= 1e-12
+        p.check()

@@ -273,3 +273,39 @@ def test_automatic_layout_rule(gpu):
                 y = p.spmv(xs, kernel=kern).cpu().numpy()
                 assert oracle.rel_errors(y, ydd)[0] <= FP64_TOL, (name, kern)
             p.check()
+
+
+def test_back_to_back_spmv_overwrites_y(gpu):
+    """y = A x launched back to back with no synchronisation in between (the
+    y-zeroing and SpMV launches overlap their start-up): every call
+    overwrites whatever y held, accumulate adds, and the reported launch
+    count matches the layout (one launch when the band owns every row)."""
+    import torch
+
+    from fastload_gb300 import gen, sweep
+
+    cases = [("random rows", gen.diag_poisson(20000, seed=3), 2),
+             ("stencil", gen.laplacian7(24), 1),
+             ("skewed rows", sweep._gen_family(4, 20000, 3.0), None),
+             ("dense columns", gen.zipf_columns(40000, 1.8, 5000, seed=3), 2)]
+    for name, c, launches in cases:
+        ydd = oracle.csc_spmv_dd(c.m, c.n, c.colptr, c.rowidx, c.val, c.x)
+        with gpu.Plan.from_csc(c.m, c.n, c.colptr, c.rowidx, c.val) as p:
+            if launches is not None:
+                assert p.info["spmv_launches"] == launches, (name, p.info)
+            xs = p.permute_x(torch.from_numpy(c.x).cuda())
+            y = torch.full((c.m,), float("nan"), dtype=torch.float64, device="cuda")
+            y2 = torch.full((c.m,), float("nan"), dtype=torch.float64, device="cuda")
+            for _ in range(3):
+                p.spmv(xs, y)
+                p.spmv(xs, y, accumulate=True)
+                p.spmv(xs, y2)
+            fid = p.add_form(gpu.VALUES_F64)
+            y3 = torch.full((c.m,), float("nan"), dtype=torch.float64, device="cuda")
+            for _ in range(3):
+                p.spmv_form(fid, xs, y3)
+            torch.cuda.synchronize()
+            assert oracle.rel_errors(y.cpu().numpy() / 2, ydd)[0] <= FP64_TOL, name
+            assert oracle.rel_errors(y2.cpu().numpy(), ydd)[0] <= FP64_TOL, name
+            assert oracle.rel_errors(y3.cpu().numpy(), ydd)[0] <= FP64_TOL, name
+            p.check()
