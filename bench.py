@@ -550,7 +550,7 @@ def run_gpu(args, rank, world):
             dist.destroy_process_group()
         return
     cpu = cpu_baseline_sample(c, budget_s=1.0 if args.quick else 12.0) if world == 1 else None
-    kname = "k_spmv_form<double,1,1,1,double,1>" if plan.info["heavy_cols"] else "k_spmv_stream_f64"
+    kname = "k_spmv_form<double,1,1,1,double,1,0>" if plan.info["heavy_cols"] else "k_spmv_stream_f64"
     traffic = ncu_traffic(kname, workload_name(n))
     plan.check()
     line = {

@@ -123,7 +123,9 @@ bool make_units(const std::vector<int> &sp, long per_unit, std::vector<int> &uni
     unit_step.clear();
     unit_slice.clear();
     const int ns = (int)sp.size() - 1;
-    per_unit = std::max(per_unit, 1024L);  // below ~32 steps a unit costs more to claim than to run
+    // at least 8 steps a unit: below that a unit costs more to claim than to
+    // run; small bands still spread over every SM
+    per_unit = std::max(per_unit, 256L);
     bool split = false, open = false;
     long acc = 0;
     for (int q = 0; q < ns; q++) {
@@ -183,6 +185,8 @@ int build_bucket(Bucket &B, int m, int n, int nnz, const int *sortnnz, const int
     FL_TRY(scan_exclusive(sortnnz, scolptr.get(), n, scolptr.get() + n, s));
     int nnz_l = 0;
     FL_TRY(read_ints(s, scolptr.get() + H0, &nnz_l, 1));
+    B.light.item_basis = nnz;  // light items sized for the whole matrix (a small light part of a large
+                               // matrix keeps large items: fewer run-boundary atomics and claims)
     FL_TRY(build_layout_device(B.light, m, H0, nnz_l, sortnnz, srow_tmp, sval_tmp, false, s, nullptr, nullptr));
     HeavyBand &H = B.heavy;
     H.H0 = H0;

@@ -86,7 +86,7 @@ struct StepTable {
 
 // Work items for the streaming SpMV kernels.  A region is the full-chunk
 // part or the partial-chunk part of one step; items cut regions into pieces
-// of at most FL_ITEM nonzeros whose interior boundaries sit on multiples of
+// of at most item_nnz_for(nnz) nonzeros whose interior boundaries sit on multiples of
 // four, so 128-bit loads stay aligned.
 struct RegionDesc {
     int start;     // first nonzero of the region (stream position)
@@ -122,6 +122,9 @@ struct Layout {
     DevBuf<int> sortrowindex;
     DevBuf<int> countrow, segmentoffset;
     Regions regions;
+    // nonzeros the work-item size is chosen for (item_nnz_for): the whole
+    // matrix's, also for the light part of a bucketed split (0: nnz)
+    long item_basis = 0;
 };
 
 // Heavy band of the bucketed form: the nh densest sorted columns, stored as
@@ -151,8 +154,8 @@ struct HeavyBand {
 
 // Work units over slices whose entry offsets are sp (nslices+1, multiples
 // of 32): consecutive short slices grouped to about per_unit entries (at
-// least 1,024),
-// slices longer than twice that cut into pieces of about per_unit entries.
+// least 256), slices longer than twice that cut into pieces of about
+// per_unit entries.
 // Returns true when a slice was cut.
 bool make_units(const std::vector<int> &sp, long per_unit, std::vector<int> &unit_step,
                 std::vector<int> &unit_slice);
@@ -195,7 +198,9 @@ __device__ __forceinline__ int upper_index(const int *__restrict__ a, int cnt, i
 }
 
 constexpr int FL_PAD = 512;     // stream padding granularity (entries)
-constexpr int FL_ITEM = 2048;   // nonzeros per work item of the stream kernel
+constexpr int FL_ITEM = 2048;   // largest work item of the stream kernel (nonzeros)
+// Work item size of a layout with nnz nonzeros (item_nnz_for in fl_prep.cu).
+int item_nnz_for(long nnz);
 
 inline size_t padded(size_t n) { return ((n + FL_PAD - 1) / FL_PAD + 1) * FL_PAD; }
 

@@ -755,9 +755,9 @@ int permute_x(const int *perm, int n, const double *x, double *xs, cudaStream_t 
 
 // ------------------------------------------------------------- regions --
 // Region 2s is the full-chunk part of step s, region 2s+1 its partial last
-// chunk; items cut each region into pieces of at most FL_ITEM nonzeros with
+// chunk; items cut each region into pieces of at most `item` nonzeros with
 // interior boundaries on multiples of four.
-__global__ void k_region_fill(StepView st, int n, RegionDesc *reg, int *pieces, int *ends) {
+__global__ void k_region_fill(StepView st, int n, int item, RegionDesc *reg, int *pieces, int *ends) {
     for (long s = blockIdx.x * (long)blockDim.x + threadIdx.x; s < st.steps; s += (long)gridDim.x * blockDim.x) {
         int cs = st.col[s], ts = st.tall[s], off = st.nnz_off[s], off1 = st.nnz_off[s + 1];
         int rem = n - cs, nfull = rem >> 5, lenp = rem & 31;
@@ -769,27 +769,35 @@ __global__ void k_region_fill(StepView st, int n, RegionDesc *reg, int *pieces, 
         ends[2 * s] = mid;
         ends[2 * s + 1] = off1;
         int A0 = off & ~3, A1 = mid & ~3;
-        pieces[2 * s] = mid > off ? (mid - A0 + FL_ITEM - 1) / FL_ITEM : 0;
-        pieces[2 * s + 1] = off1 > mid ? (off1 - A1 + FL_ITEM - 1) / FL_ITEM : 0;
+        pieces[2 * s] = mid > off ? (mid - A0 + item - 1) / item : 0;
+        pieces[2 * s + 1] = off1 > mid ? (off1 - A1 + item - 1) / item : 0;
     }
 }
 
 __global__ void k_item_fill(const RegionDesc *reg, const int *ends, const int *poff, int nreg, int nitems,
-                            ItemDesc *items) {
+                            int item, ItemDesc *items) {
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < nitems; i += (long)gridDim.x * blockDim.x) {
         int r = upper_index(poff, nreg, (int)i);
         int rs = reg[r].start, re = ends[r];
         int A = rs & ~3;
         int j = (int)i - poff[r];
-        int b = max(rs, A + j * FL_ITEM);
-        int e = min(re, A + (j + 1) * FL_ITEM);
+        int b = max(rs, A + j * item);
+        int e = min(re, A + (j + 1) * item);
         items[i] = ItemDesc{b, e, r, 0};
     }
+}
+
+int item_nnz_for(long nnz) {
+    // about two items per warp of the GPU, so a small matrix still spreads
+    // over every SM; at most FL_ITEM, at least 128 (and a multiple of it)
+    const long per = (nnz + 2L * num_sms() * 32 - 1) / (2L * num_sms() * 32);
+    return (int)std::min<long>(FL_ITEM, std::max<long>(128, (per + 127) / 128 * 128));
 }
 
 int build_regions(Layout &L, cudaStream_t s) {
     StepTable &st = L.st;
     Regions &R = L.regions;
+    const int item = item_nnz_for(L.item_basis > 0 ? L.item_basis : L.nnz);
     int nreg = 2 * st.steps;
     R.nregions = nreg;
     R.nitems = 0;
@@ -800,7 +808,7 @@ int build_regions(Layout &L, cudaStream_t s) {
     FL_TRY(ends.alloc(nreg, s));
     FL_TRY(poff.alloc(nreg + 1, s));
     StepView sv{st.col.get(), st.base.get(), st.tall.get(), st.tile_off.get(), st.nnz_off.get(), st.steps};
-    k_region_fill<<<grid_for(st.steps, 256), 256, 0, s>>>(sv, L.n, R.region.get(), pieces.get(), ends.get());
+    k_region_fill<<<grid_for(st.steps, 256), 256, 0, s>>>(sv, L.n, item, R.region.get(), pieces.get(), ends.get());
     FL_CUDA(cudaGetLastError());
     FL_TRY(scan_exclusive(pieces.get(), poff.get(), nreg, poff.get() + nreg, s));
     int nitems = 0;
@@ -808,7 +816,7 @@ int build_regions(Layout &L, cudaStream_t s) {
     R.nitems = nitems;
     if (nitems == 0) return FL_SUCCESS;
     FL_TRY(R.item.alloc(nitems, s));
-    k_item_fill<<<grid_for(nitems, 256), 256, 0, s>>>(R.region.get(), ends.get(), poff.get(), nreg, nitems,
+    k_item_fill<<<grid_for(nitems, 256), 256, 0, s>>>(R.region.get(), ends.get(), poff.get(), nreg, nitems, item,
                                                       R.item.get());
     FL_CUDA(cudaGetLastError());
     return FL_SUCCESS;

@@ -19,6 +19,9 @@
 #include "fl_stream.cuh"
 
 #include <algorithm>
+#include <map>
+#include <mutex>
+#include <utility>
 
 namespace fl {
 
@@ -80,8 +83,24 @@ __global__ void __launch_bounds__(256) k_spmv_tile_f64(int tilenum, const int *_
 }
 
 static int occupancy_grid(const void *fn, int threads, long work_warps) {
+    // resident blocks per SM of (kernel, block size): queried once, the query
+    // costs host time on every call otherwise
+    static std::mutex mu;
+    static std::map<std::pair<const void *, int>, int> cache;
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, 0);
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        auto it = cache.find({fn, threads});
+        if (it != cache.end()) {
+            per_sm = it->second;
+        } else {
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, 0) != cudaSuccess) {
+                cudaGetLastError();
+                per_sm = 0;
+            }
+            if (per_sm > 0) cache[{fn, threads}] = per_sm;
+        }
+    }
     if (per_sm <= 0) per_sm = 1;
     long g = (long)num_sms() * per_sm;
     long need = (work_warps * 32 + threads - 1) / threads;
