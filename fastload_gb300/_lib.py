@@ -89,6 +89,7 @@ SIGNATURES = [
     ("fl_plan_permute_x", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("fl_plan_spmv", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p]),
     ("fl_plan_spmv_host", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
+    ("fl_plan_spmv_host_async", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
     ("fl_plan_destroy", C.c_int, [C.c_void_p]),
     ("fl_mtx_read", C.c_int, [C.POINTER(C.c_void_p), C.c_char_p, C.c_void_p]),
     ("fl_mtx_info_get", C.c_int, [C.c_void_p, C.POINTER(MtxInfoC)]),

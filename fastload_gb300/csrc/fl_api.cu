@@ -620,6 +620,47 @@ int fl_plan_spmv_host(fl_plan_t p, const double *h_xs, double *h_y, int variant,
     return FL_SUCCESS;
 }
 
+int fl_plan_spmv_host_async(fl_plan_t p, const double *h_xs, double *h_y, int variant, void *stream) {
+    clear_error();
+    if (!p || (p->L.n && !h_xs) || (p->L.m && !h_y)) return fail(FL_ERR_ARG, "plan_spmv_host_async: NULL argument");
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!p->up_s) {
+        FL_CUDA(cudaStreamCreateWithFlags(&p->up_s, cudaStreamNonBlocking));
+        FL_CUDA(cudaStreamCreateWithFlags(&p->comp_s, cudaStreamNonBlocking));
+        FL_CUDA(cudaStreamCreateWithFlags(&p->down_s, cudaStreamNonBlocking));
+        for (fl_plan::AsyncSlot &a : p->slot) {
+            FL_CUDA(cudaEventCreateWithFlags(&a.up, cudaEventDisableTiming));
+            FL_CUDA(cudaEventCreateWithFlags(&a.kdone, cudaEventDisableTiming));
+            FL_CUDA(cudaEventCreateWithFlags(&a.down, cudaEventDisableTiming));
+        }
+    }
+    fl_plan::AsyncSlot &S = p->slot[p->slot_next];
+    if (S.x.n < (size_t)p->L.n) FL_TRY(S.x.alloc(p->L.n, s));
+    if (S.y.n < (size_t)p->L.m) FL_TRY(S.y.alloc(p->L.m, s));
+    // The upload does not wait for earlier work on `stream`: that stream
+    // waits for every earlier call's result, so ordering after it would
+    // serialise the pipeline.  h_xs is read as it stands at the call.
+    // upload: into the slot once the kernel two calls back has read it
+    if (S.used) FL_CUDA(cudaStreamWaitEvent(p->up_s, S.kdone, 0));
+    if (p->L.n)
+        FL_CUDA(cudaMemcpyAsync(S.x.get(), h_xs, (size_t)p->L.n * sizeof(double), cudaMemcpyHostToDevice, p->up_s));
+    FL_CUDA(cudaEventRecord(S.up, p->up_s));
+    // compute: once x is in and the download two calls back has read y
+    FL_CUDA(cudaStreamWaitEvent(p->comp_s, S.up, 0));
+    if (S.used) FL_CUDA(cudaStreamWaitEvent(p->comp_s, S.down, 0));
+    FL_TRY(fl_plan_spmv(p, S.x.get(), S.y.get(), 0, variant, p->comp_s));
+    FL_CUDA(cudaEventRecord(S.kdone, p->comp_s));
+    // download, and the caller's stream waits for it
+    FL_CUDA(cudaStreamWaitEvent(p->down_s, S.kdone, 0));
+    if (p->L.m)
+        FL_CUDA(cudaMemcpyAsync(h_y, S.y.get(), (size_t)p->L.m * sizeof(double), cudaMemcpyDeviceToHost, p->down_s));
+    FL_CUDA(cudaEventRecord(S.down, p->down_s));
+    FL_CUDA(cudaStreamWaitEvent(s, S.down, 0));
+    S.used = true;
+    p->slot_next ^= 1;
+    return FL_SUCCESS;
+}
+
 int fl_plan_add_form(fl_plan_t p, int value_type, int heavy_band, int y_f32, int *form_id) {
     clear_error();
     if (!p || !form_id) return fail(FL_ERR_ARG, "add_form: NULL argument");

@@ -317,6 +317,18 @@ struct fl_plan {
     int *epoch_host = nullptr;                   // pinned, mapped: [0] epoch, [1] status
     int *epoch_dev = nullptr;                    // device view of epoch_host
     int epoch = 0;
+    // fl_plan_spmv_host_async: two device staging slots used in turn, an
+    // upload, a compute and a download stream.  A slot's x is overwritten
+    // once the kernel that read it is done (kdone), its y once the copy that
+    // read it is done (down).
+    struct AsyncSlot {
+        fl::DevBuf<double> x, y;
+        cudaEvent_t up = nullptr, kdone = nullptr, down = nullptr;
+        bool used = false;
+    };
+    AsyncSlot slot[2];
+    int slot_next = 0;
+    cudaStream_t up_s = nullptr, comp_s = nullptr, down_s = nullptr;
     fl_plan() = default;
     fl_plan(const fl_plan &) = delete;
     fl_plan &operator=(const fl_plan &) = delete;
@@ -325,5 +337,10 @@ struct fl_plan {
         if (fork) cudaEventDestroy(fork);
         if (join) cudaEventDestroy(join);
         if (epoch_host) cudaFreeHost(epoch_host);
+        for (AsyncSlot &a : slot)
+            for (cudaEvent_t e : {a.up, a.kdone, a.down})
+                if (e) cudaEventDestroy(e);
+        for (cudaStream_t st : {up_s, comp_s, down_s})
+            if (st) cudaStreamDestroy(st);
     }
 };

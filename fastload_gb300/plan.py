@@ -216,6 +216,23 @@ class Plan:
                                        int(kernel), _stream_handle(stream)))
         return y
 
+    def spmv_host_async(self, xs: np.ndarray, y: np.ndarray, kernel: int = KERNEL_AUTO, stream=None) -> np.ndarray:
+        """Pipelined host-buffer SpMV: enqueues H2D of xs, y = A xs and D2H
+        into y, and returns at once; y is valid after the stream (torch's
+        current stream by default) is synchronised.  Consecutive calls
+        overlap their copies with the kernels.  xs must hold x when called
+        (the upload does not wait for earlier work on the stream); xs and y
+        must be C-contiguous float64 arrays that stay alive, unmodified (xs)
+        and unread (y) until then; pinned memory (torch pin_memory) lets the
+        copies overlap."""
+        if xs.dtype != np.float64 or y.dtype != np.float64 or not xs.flags.c_contiguous or not y.flags.c_contiguous:
+            raise ValueError("spmv_host_async needs C-contiguous float64 arrays")
+        if xs.size < self.n or y.size < self.m:
+            raise ValueError("spmv_host_async: xs needs n and y m elements")
+        check(load().fl_plan_spmv_host_async(self._h, C.c_void_p(xs.ctypes.data), C.c_void_p(y.ctypes.data),
+                                             int(kernel), _stream_handle(stream)))
+        return y
+
     # -- forms ---------------------------------------------------------------
     def add_form(self, value_type: int = VALUES_F32, heavy_band: int = BAND_AUTO, y_f32: bool = False) -> int:
         """Adds a storage form (FP64 / FP32 / BF16 hi+lo values) with the given

@@ -200,6 +200,19 @@ int fl_plan_spmv(fl_plan_t plan, const double *d_xs, double *d_y,
  * Pinned host buffers give the fastest copies. */
 int fl_plan_spmv_host(fl_plan_t plan, const double *h_xs, double *h_y,
                       int variant, void *stream);
+/* Pipelined host-buffer SpMV: enqueues the copy of xs to the device, y = A xs
+ * and the copy of y back, and returns without waiting; `stream` waits for
+ * the result, so synchronising it (or an event recorded on it after this
+ * call) makes h_y valid.  Consecutive calls overlap: the upload of one x and
+ * the download of an earlier y run while a kernel computes (three internal
+ * streams, two device staging slots reused in turn once the call that used
+ * a slot two calls earlier has finished with it).  The upload does not wait
+ * for earlier work on `stream`: h_xs must hold x when the call is made, and
+ * may be reused, like h_y read, only after that synchronisation.  Both
+ * should be pinned (page-locked) host memory, otherwise the copies are
+ * synchronous and nothing overlaps. */
+int fl_plan_spmv_host_async(fl_plan_t plan, const double *h_xs, double *h_y,
+                            int variant, void *stream);
 int fl_plan_destroy(fl_plan_t plan);
 /* Reads and clears the device status word of the plan's kernels (0 when no
  * bounded wait expired); synchronises the device. */
