@@ -236,10 +236,17 @@ int build_bucket(Bucket &B, int m, int n, int nnz, const int *sortnnz, const int
     int total = 0;
     FL_TRY(read_ints(s, H.slice_ptr.get() + H.nslices, &total, 1));
     H.padded = total;
-    FL_TRY(H.val.alloc(std::max(total, 1), s));
+    // one ring stage of zeros past the end (the ring kernels copy whole stages)
+    FL_TRY(H.val.alloc((size_t)total + RING_PAD, s));
+    FL_CUDA(cudaMemsetAsync(H.val.get() + total, 0, RING_PAD * sizeof(double), s));
     const bool narrow = nh <= 65535;
-    if (narrow) FL_TRY(H.col.alloc(std::max(total, 1), s));
-    else FL_TRY(H.col32.alloc(std::max(total, 1), s));
+    if (narrow) {
+        FL_TRY(H.col.alloc((size_t)total + RING_PAD, s));
+        FL_CUDA(cudaMemsetAsync(H.col.get() + total, 0, RING_PAD * sizeof(uint16_t), s));
+    } else {
+        FL_TRY(H.col32.alloc((size_t)total + RING_PAD, s));
+        FL_CUDA(cudaMemsetAsync(H.col32.get() + total, 0, RING_PAD * sizeof(int), s));
+    }
     FL_TRY(H.row.alloc(32L * H.nslices, s));
     FL_TRY(H.len.alloc(32L * H.nslices, s));
     // work units: about four per resident warp, so that every warp has work

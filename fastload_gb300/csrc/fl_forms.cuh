@@ -268,6 +268,9 @@ template <typename V>
 __host__ __device__ constexpr int ring_warp_bytes() {
     return RING_STAGES * ring_stage_bytes<V>();
 }
+// Entries of zero padding past the end of a band's value and column arrays:
+// the ring copies whole stages.
+constexpr int RING_PAD = RING_STEPS * 32;
 
 __device__ __forceinline__ void cp_async16(void *smem_dst, const void *gsrc) {
     const uint32_t d = (uint32_t)__cvta_generic_to_shared(smem_dst);
@@ -279,36 +282,36 @@ __device__ __forceinline__ void cp_async_wait() {
     asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
-// Stage k (steps RING_STEPS*k ...) of the unit starting at entry E0 with T
-// steps into ring slot k % RING_STAGES; always commits a group (empty past
-// the end) so the per-thread group count stays in step with k.
-template <typename V>
-__device__ __forceinline__ void ring_issue(unsigned char *ring, const V *hval, const uint16_t *hcol, int E0, int T,
-                                           int k, int lane) {
-    const int t0 = k * RING_STEPS;
-    const int steps = min(RING_STEPS, T - t0);
-    if (steps > 0) {
-        unsigned char *slot = ring + (k % RING_STAGES) * ring_stage_bytes<V>();
-        const int vbytes = steps * 32 * (int)sizeof(V), cbytes = steps * 64;
-        const char *vsrc = (const char *)(hval + E0 + 32 * t0);
-        const char *csrc = (const char *)(hcol + E0 + 32 * t0);
-        for (int off = lane * 16; off < vbytes; off += 512) cp_async16(slot + off, vsrc + off);
-        unsigned char *cdst = slot + RING_STEPS * 32 * sizeof(V);
-        for (int off = lane * 16; off < cbytes; off += 512) cp_async16(cdst + off, csrc + off);
-    }
-    cp_async_commit();
-}
-
 template <typename V, typename Y>
 __device__ __forceinline__ void heavy_unit_ring(const FormArgs<V, Y> &a, int sl, int T0, int T1,
                                                 const typename VT<V>::X *xsrc, unsigned char *ring, int lane) {
     using A = typename VT<V>::A;
     if (T0 >= T1) return;
-    const int E0 = 32 * T0;  // first entry of the unit
-    const int T = T1 - T0;   // its steps
+    constexpr int VB = RING_STEPS * 32 * (int)sizeof(V);  // value bytes of a stage
+    constexpr int CB = RING_STEPS * 32 * (int)sizeof(uint16_t);  // column bytes of a stage
+    constexpr int SB = ring_stage_bytes<V>();
+    const int T = T1 - T0;  // the unit's steps
     const int nst = (T + RING_STEPS - 1) / RING_STEPS;
+    // Stage k (steps RING_STEPS*k ...) goes to ring slot k % RING_STAGES,
+    // always whole: a unit's last stage may run into the next unit's steps
+    // or, for the band's last unit, the stage of zero padding the band
+    // arrays carry past their end; the consumer stops at T.  Every call
+    // commits a group (empty past the unit) so the per-thread group count
+    // stays in step with k.  This lane's 16-byte pieces are fixed offsets.
+    const char *vsrc = (const char *)(a.hval + 32 * (size_t)T0);
+    const char *csrc = (const char *)(a.hcol16 + 32 * (size_t)T0);
+    auto issue = [&](int k) {
+        if (k < nst) {
+            unsigned char *slot = ring + (k % RING_STAGES) * SB;
 #pragma unroll
-    for (int k = 0; k < RING_STAGES; k++) ring_issue<V>(ring, a.hval, a.hcol16, E0, T, k, lane);
+            for (int off = 0; off < VB; off += 512)
+                if (off + lane * 16 < VB) cp_async16(slot + off + lane * 16, vsrc + (size_t)k * VB + off + lane * 16);
+            if (lane * 16 < CB) cp_async16(slot + VB + lane * 16, csrc + (size_t)k * CB + lane * 16);
+        }
+        cp_async_commit();
+    };
+#pragma unroll
+    for (int k = 0; k < RING_STAGES; k++) issue(k);
     const int base = __ldg(a.slice_ptr + sl);
     int bnd = (__ldg(a.slice_ptr + sl + 1) >> 5) - T0;  // unit step where the slice ends
     int len = __ldg(a.hlen + 32 * sl + lane), r = __ldg(a.hrow + 32 * sl + lane);
@@ -323,40 +326,50 @@ __device__ __forceinline__ void heavy_unit_ring(const FormArgs<V, Y> &a, int sl,
     for (int k = 0; k < nst; k++) {
         cp_async_wait<RING_STAGES - 1>();
         __syncwarp();
-        const unsigned char *slot = ring + (k % RING_STAGES) * ring_stage_bytes<V>();
+        const unsigned char *slot = ring + (k % RING_STAGES) * SB;
         const V *sv = (const V *)slot;
-        const uint16_t *sc = (const uint16_t *)(slot + RING_STEPS * 32 * sizeof(V));
+        const uint16_t *sc = (const uint16_t *)(slot + VB);
+        const int t0 = k * RING_STEPS;
+        if (t0 + RING_STEPS < bnd && t0 + RING_STEPS < T) {
+            // no slice end and no unit end inside this stage
 #pragma unroll
-        for (int q = 0; q < RING_STEPS; q++) {
-            const int t = k * RING_STEPS + q;
-            if (t < T) {
-                if (j < len) {
-                    const A v = VT<V>::plain1(sv + 32 * q + lane);  // shared memory
-                    acc[0] = fma(v, (A)xsrc[sc[32 * q + lane]], acc[0]);
-                }
-                j++;
-                const bool slice_end = t + 1 == bnd;
-                if (slice_end || t + 1 == T) {
-                    if (len > jb) heavy_flush<A, 1, Y>(a.heavy_mode, a.y, r, acc);
-                    acc[0] = (A)0;
-                    if (slice_end) {
-                        sl++;
-                        j = 0;
-                        jb = 0;
-                        len = nlen;
-                        r = nr;
-                        bnd = nbnd;
-                        if (bnd < T) {
-                            nbnd = (__ldg(a.slice_ptr + sl + 2) >> 5) - T0;
-                            nlen = __ldg(a.hlen + 32 * (sl + 1) + lane);
-                            nr = __ldg(a.hrow + 32 * (sl + 1) + lane);
+            for (int q = 0; q < RING_STEPS; q++)
+                if (j + q < len)
+                    acc[0] = fma(VT<V>::plain1(sv + 32 * q + lane), (A)xsrc[sc[32 * q + lane]], acc[0]);
+            j += RING_STEPS;
+        } else {
+#pragma unroll
+            for (int q = 0; q < RING_STEPS; q++) {
+                const int t = t0 + q;
+                if (t < T) {
+                    if (j < len) {
+                        const A v = VT<V>::plain1(sv + 32 * q + lane);  // shared memory
+                        acc[0] = fma(v, (A)xsrc[sc[32 * q + lane]], acc[0]);
+                    }
+                    j++;
+                    const bool slice_end = t + 1 == bnd;
+                    if (slice_end || t + 1 == T) {
+                        if (len > jb) heavy_flush<A, 1, Y>(a.heavy_mode, a.y, r, acc);
+                        acc[0] = (A)0;
+                        if (slice_end) {
+                            sl++;
+                            j = 0;
+                            jb = 0;
+                            len = nlen;
+                            r = nr;
+                            bnd = nbnd;
+                            if (bnd < T) {
+                                nbnd = (__ldg(a.slice_ptr + sl + 2) >> 5) - T0;
+                                nlen = __ldg(a.hlen + 32 * (sl + 1) + lane);
+                                nr = __ldg(a.hrow + 32 * (sl + 1) + lane);
+                            }
                         }
                     }
                 }
             }
         }
         __syncwarp();
-        ring_issue<V>(ring, a.hval, a.hcol16, E0, T, k + RING_STAGES, lane);
+        issue(k + RING_STAGES);
     }
     cp_async_wait<0>();
     __syncwarp();
