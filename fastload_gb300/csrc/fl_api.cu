@@ -221,6 +221,7 @@ int upload_layout(Layout &L, const fl_slide_matrix *mat, int m, int n, int nnz, 
     FL_TRY(build_steps(L, m, n, nnz, cnt.get(), s));
     if (L.tilenum != T) return fail(FL_ERR_ARG, "FastLoad_spmv: tilenum=%d but the tiles imply %d", T, L.tilenum);
     FL_TRY(check_tile_meta(L, tptr.get(), tlen.get(), tcol.get(), s));
+    L.sortnnz = std::move(cnt);  // nnz per sorted column (the staircase the tiles were checked against)
     return FL_SUCCESS;
 }
 
@@ -336,27 +337,53 @@ int fl_fastload_spmv(const fl_slide_matrix *matrix, int nnz, int colA, int rowA,
     cudaStream_t s = 0;
     Layout L;
     FL_TRY(upload_layout(L, matrix, rowA, colA, nnz, s));
+    // The bucketed split of the uploaded layout when it has a band of dense
+    // columns (the plans' first rule; their second, rows as slices for local
+    // or row-skewed matrices, needs the column permutation, which a
+    // slide_matrix does not carry): the densest columns as row slices, the
+    // rest as the FastLoad stream; else the FastLoad stream kernel.
+    Bucket B;
+    int nh = 0;
+    if (nnz > 0) {
+        nh = bucket_auto_band(L.sortnnz.get(), colA, nnz, s);
+        if (nh < 0) return nh;
+    }
+    if (nh > 0) {
+        DevBuf<int> srow;
+        DevBuf<double> sval;
+        FL_TRY(untile_layout(L, srow, sval, s));
+        FL_TRY(build_bucket(B, rowA, colA, nnz, L.sortnnz.get(), srow.get(), sval.get(), nh, s));
+    }
     DevBuf<double> dx, dy;
     FL_TRY(upload(dx, x_sorted, colA, s));
     FL_TRY(dy.alloc(rowA, s));
+    auto run = [&]() -> int {
+        return nh > 0 ? spmv_bucket_f64(B, dx.get(), dy.get(), 1, s)
+                      : spmv_stream_f64(L, dx.get(), dy.get(), FL_KERNEL_AUTO, s);
+    };
     if (rowA) FL_CUDA(cudaMemsetAsync(dy.get(), 0, (size_t)rowA * sizeof(double), s));
-    FL_TRY(spmv_stream_f64(L, dx.get(), dy.get(), FL_KERNEL_AUTO, s));  // untimed first run
+    FL_TRY(run());  // untimed first run
     double total = 0;
     for (int r = 0; r < reps; r++) {
         if (rowA) FL_CUDA(cudaMemsetAsync(dy.get(), 0, (size_t)rowA * sizeof(double), s));
         Timer t;
         double ms = 0;
         FL_TRY(t.start(s));
-        FL_TRY(spmv_stream_f64(L, dx.get(), dy.get(), FL_KERNEL_AUTO, s));
+        FL_TRY(run());
         FL_TRY(t.stop(s, &ms));
         total += ms;
     }
     if (reps == 0 && rowA) {
         FL_CUDA(cudaMemsetAsync(dy.get(), 0, (size_t)rowA * sizeof(double), s));
-        FL_TRY(spmv_stream_f64(L, dx.get(), dy.get(), FL_KERNEL_AUTO, s));
+        FL_TRY(run());
     }
     FL_TRY(download(y, dy.get(), rowA, s));
     FL_CUDA(cudaStreamSynchronize(s));
+    if (nh > 0) {
+        int h = 0;
+        FL_CUDA(cudaMemcpy(&h, B.err.get(), sizeof(int), cudaMemcpyDeviceToHost));
+        if (h) return fail(FL_ERR_NOT_READY, "FastLoad_spmv: a bounded device wait expired (0x%x)", h);
+    }
     if (ms_per_spmv) *ms_per_spmv = reps ? total / reps : 0.0;
     if (mismatches) {
         int bad = 0;

@@ -309,3 +309,32 @@ def test_back_to_back_spmv_overwrites_y(gpu):
             assert oracle.rel_errors(y2.cpu().numpy(), ydd)[0] <= FP64_TOL, name
             assert oracle.rel_errors(y3.cpu().numpy(), ydd)[0] <= FP64_TOL, name
             p.check()
+
+
+def test_dropin_fastload_spmv_runs_the_bucketed_kernel(gpu):
+    """The reference's call sequence (csr_to_csc -> ColSort ->
+    formatTransform -> FastLoad_spmv) on a matrix with dense columns: the
+    drop-in FastLoad_spmv builds the bucketed split from the slide_matrix and
+    its product matches the oracle; on integer data it is exact (the
+    reference's own check counts no mismatch)."""
+    import scipy.sparse as sp
+
+    from fastload_gb300 import gen
+
+    c = gen.zipf_columns(40000, 1.8, 5000, seed=3)
+    A = sp.csc_matrix((c.val, c.rowidx, c.colptr), shape=(c.m, c.n)).tocsr()
+    rp, ci = A.indptr.astype(np.int32), A.indices.astype(np.int32)
+    for integer in (False, True):
+        val = np.round(A.data * 4) if integer else A.data
+        x = np.round(c.x * 8) if integer else c.x
+        t, cv, cr, cp, cnt = gpu.csr_to_csc(c.m, c.n, len(val), val, rp, ci)
+        t, srow, sval, snnz, sx = gpu.ColSort(c.m, c.n, len(val), cnt, cp, cr, cv, x)
+        ta, tb, sm, h = gpu.formatTransform(srow, sval, snnz, len(val), c.m, c.n)
+        ydd = oracle.csc_spmv_dd(c.m, c.n, cp, cr, cv, x)
+        y, ms, bad = gpu.FastLoad_spmv(sm, len(val), c.n, c.m, sx, y_golden=ydd, reps=3)
+        assert ms > 0
+        if integer:
+            np.testing.assert_array_equal(y, ydd)
+            assert bad == 0
+        else:
+            assert oracle.rel_errors(y, ydd)[0] <= FP64_TOL
