@@ -105,12 +105,15 @@ int auto_layout_band(const Layout &L, int x_bytes, bool *wide, cudaStream_t s) {
         // No dense columns.  Rows as slices (every column in the band, x
         // through the cache, one y update per row part) beat the FastLoad
         // stream's atomic per nonzero when x gathers have locality (banded,
-        // block, stencil: mean |r/m - c/n| small) or when rows are skewed
-        // (hot rows make the stream's atomics collide; cut slices spread
-        // them over units).
+        // block, stencil: mean |r/m - c/n| small), when rows are skewed (hot
+        // rows make the stream's atomics collide; cut slices spread them
+        // over units), and on large matrices of several nonzeros a column,
+        // where the stream's random atomics bound it (1.5x at 5M+ uniformly
+        // random nonzeros; below 1M the stream's lower fixed cost wins).
         float f[24];
         FL_TRY(plan_features(L, f, s));
-        if (f[21] < 0.05f || f[22] > 2.0f) {
+        const bool big = L.nnz >= 1000000 && (long)L.nnz >= 4L * L.n;
+        if (f[21] < 0.05f || f[22] > 2.0f || big) {
             nh = L.n;
             *wide = true;
         }

@@ -281,8 +281,9 @@ int bucket_auto_band(const int *sortnnz, int n, int nnz, cudaStream_t s, int x_b
 int plan_features(const Layout &L, float *out, cudaStream_t s);
 // The automatic heavy band of a layout: the densest columns when they hold
 // enough of the matrix; with none, every column as row slices when x
-// gathers have locality or rows are skewed; else no band (0).  *wide is set
-// when the band is wider than shared memory holds x for.
+// gathers have locality, rows are skewed, or the matrix has 1M+ nonzeros and
+// 4+ a column; else no band (0).  *wide is set when the band is wider than
+// shared memory holds x for.
 int auto_layout_band(const Layout &L, int x_bytes, bool *wide, cudaStream_t s);
 
 int num_sms();

@@ -142,7 +142,8 @@ typedef struct fl_plan_opts {
                         0 automatic (the densest columns with >= 32 nonzeros,
                         at most 16384, when they hold >= 1/4 of the matrix;
                         with none, every column as row slices when x gathers
-                        have locality or rows are skewed; else off), > 0 that
+                        have locality, rows are skewed or the matrix has 1M+
+                        nonzeros and 4+ a column; else off), > 0 that
                         many of the densest columns (even, at most
                         fl_plan_max_heavy_band()) */
     int reserved[6];
@@ -329,7 +330,7 @@ int fl_cusparse_spmv_host(int m, int n, int nnz, const int *csr_rowptr,
 #define FL_VALUES_F32 1    /* FP32 values, FP32 x, FP32 products */
 #define FL_VALUES_BF16X2 2 /* BF16 hi+lo split (v ~ hi + lo), FP32 x, FP32 products */
 /* Heavy band of a form (columns handled in 32-row slices, one lane per row). */
-#define FL_BAND_AUTO 0     /* automatic: the densest columns (>= 32 nonzeros, up to 128 KB of x: 16,384 FP64 / 32,768 FP32 columns) when they hold >= 1/4 of the matrix; else every column when x gathers have locality or rows are skewed; else none */
+#define FL_BAND_AUTO 0     /* automatic: the densest columns (>= 32 nonzeros, up to 128 KB of x: 16,384 FP64 / 32,768 FP32 columns) when they hold >= 1/4 of the matrix; else every column when x gathers have locality, rows are skewed or the matrix has 1M+ nonzeros and 4+ a column; else none */
 #define FL_BAND_NONE (-1)  /* pure FastLoad tile stream (one atomic per run) */
 #define FL_BAND_ALL (-2)   /* every column: rows owned by one lane, no atomics */
 

@@ -255,6 +255,7 @@ def test_automatic_layout_rule(gpu):
     from fastload_gb300 import gen, sweep
 
     cases = [("random rows", gen.diag_poisson(20000, seed=3), 0),
+             ("random rows, 1M+ nonzeros, 5 a column", gen.diag_poisson(1 << 18, seed=3), "all"),
              ("stencil", gen.laplacian7(24), "all"),
              ("skewed rows", sweep._gen_family(4, 20000, 3.0), "all"),
              ("dense columns", gen.zipf_columns(40000, 1.8, 5000, seed=3), "band")]
