@@ -32,6 +32,10 @@ def matrices(gpu):
     yield "poisson", c.m, c.n, c.colptr, c.rowidx, c.val
     c = gen.zipf_columns(40000, 1.8, 5000, seed=3)
     yield "zipf", c.m, c.n, c.colptr, c.rowidx, c.val
+    # the automatic rule puts every column of a stencil in the band (x read
+    # through the cache): the file records it and the load rebuilds it wide
+    c = gen.laplacian7(16)
+    yield "stencil", c.m, c.n, c.colptr, c.rowidx, c.val
     # empty columns and an empty matrix
     yield "empty_cols", 6, 5, np.array([0, 0, 2, 2, 5, 5]), np.array([1, 4, 0, 2, 5]), np.arange(1.0, 6.0)
     yield "empty", 4, 3, np.zeros(4, np.int64), np.zeros(0, np.int64), np.zeros(0)
@@ -55,6 +59,8 @@ def test_round_trip(gpu, tmp_path, with_ref, heavy):
                 assert P.plan_file_hash(np.ascontiguousarray(sec[k]).tobytes()) == hdr["hashes"][k], (name, k)
             with gpu.Plan.load(f) as b:
                 assert a.info == b.info, name
+                if name == "stencil" and heavy == 0:
+                    assert b.info["heavy_cols"] == n
                 if with_ref:
                     sa, pa = a.export()
                     sb, pb = b.export()
