@@ -8,10 +8,17 @@
 //  * the heavy band [H0, n) -- the densest columns, which on skewed matrices
 //    hold most of the nonzeros -- is re-packed row-major into slices of 32
 //    rows: lane l of a slice owns one row and walks its band nonzeros,
-//    accumulating value * x with one FP64 FMA each, x read from shared
-//    memory (the band's x is staged there by a TMA bulk copy at kernel start,
-//    overlapped with the light work), and adds the row's sum to y with one
-//    atomic.
+//    accumulating value * x with one FP64 FMA each, and adds the row's sum
+//    to y with one atomic.  A band of at most 16,384 columns has its x
+//    staged in shared memory by a TMA bulk copy at kernel start (overlapped
+//    with the light work) and streams its values and columns through
+//    per-warp cp.async rings; the automatic layout may also put every
+//    column in the band (x read through the cache), and then each row is
+//    owned by one lane and y is written without atomics.
+//
+// Work units are step ranges of the band (at least 256 entries, about four
+// per resident warp; long slices are cut, their parts meeting in y by
+// atomics) and light items of the tile stream, dealt to blocks round-robin.
 //
 // On GB300 scattered L2 atomics (about 221 G/s) and FP64 pipe slots (about
 // 500 G/s) are the scarce resources of a CSC SpMV; the heavy band turns one

@@ -7,7 +7,16 @@
 //   XS x of the heavy band read from shared memory (staged by a TMA bulk copy)
 //      or from global memory (bands wider than shared memory);
 //   C16 heavy-band column indices stored as 16 bits (band <= 65535) or 32;
-//   Y  y type (double, or float for the FP32-accumulating batched form).
+//   Y  y type (double, or float for the FP32-accumulating batched form);
+//   RING the band's values and columns streamed through per-warp
+//      shared-memory rings (K = 1, x in shared memory) instead of the
+//      register-pipelined loop;
+//   OVL the light columns' x still arriving when the kernel starts (the
+//      overlapped host-buffer call): heavy units first, light items once a
+//      flag says the x is in.
+// Launched as a programmatic dependent of the kernel before it (the y
+// zeroing), the kernel waits for that kernel before touching memory and
+// releases its own dependent when each block is done.
 // Products and per-row sums are computed in FP32 for the FP32/BF16 forms and
 // in FP64 for the FP64 form; y is accumulated in Y.  The work is the bucketed
 // split of fl_bucket.cu: light columns in the FastLoad tile stream with one
