@@ -18,6 +18,10 @@
  * Status codes are 0 on success and negative on failure; fl_last_error()
  * returns the message of the last failure on the calling thread.  All
  * indices are 32-bit, as in the reference (nnz < 2^31).
+ *
+ * Threads: different plans may be used from different host threads at
+ * once; one plan is used by one host thread at a time (its host-buffer
+ * calls keep staging buffers, streams and a pipelining slot counter).
  */
 #ifndef FASTLOAD_GB300_H
 #define FASTLOAD_GB300_H
