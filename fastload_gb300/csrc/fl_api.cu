@@ -662,8 +662,10 @@ int fl_plan_spmv_host_async(fl_plan_t p, const double *h_xs, double *h_y, int va
         }
     }
     fl_plan::AsyncSlot &S = p->slot[p->slot_next];
-    if (S.x.n < (size_t)p->L.n) FL_TRY(S.x.alloc(p->L.n, s));
-    if (S.y.n < (size_t)p->L.m) FL_TRY(S.y.alloc(p->L.m, s));
+    // stream-ordered allocations on the upload stream: every later use of
+    // the slot (compute, download) is ordered after the upload
+    if (S.x.n < (size_t)p->L.n) FL_TRY(S.x.alloc(p->L.n, p->up_s));
+    if (S.y.n < (size_t)p->L.m) FL_TRY(S.y.alloc(p->L.m, p->up_s));
     // The upload does not wait for earlier work on `stream`: that stream
     // waits for every earlier call's result, so ordering after it would
     // serialise the pipeline.  h_xs is read as it stands at the call.

@@ -334,6 +334,15 @@ struct fl_plan {
     fl_plan(const fl_plan &) = delete;
     fl_plan &operator=(const fl_plan &) = delete;
     ~fl_plan() {
+        // the device is idle here (fl_plan_destroy synchronises): free the
+        // host-call staging on the legacy stream, before the streams they
+        // were allocated on are destroyed (the caller's may be gone already)
+        for (fl::DevBuf<double> *b : {&stage_x, &stage_y, &slot[0].x, &slot[0].y, &slot[1].x, &slot[1].y}) {
+            b->s = 0;
+            b->release();
+        }
+        x_flag.s = 0;
+        x_flag.release();
         if (side) cudaStreamDestroy(side);
         if (fork) cudaEventDestroy(fork);
         if (join) cudaEventDestroy(join);

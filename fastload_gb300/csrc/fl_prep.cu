@@ -61,7 +61,13 @@ int dev_alloc(void **p, size_t bytes, cudaStream_t s) {
     return FL_SUCCESS;
 }
 void dev_free(void *p, cudaStream_t s) {
-    if (p) cudaFreeAsync(p, s);
+    if (!p) return;
+    // the stream it was allocated on may be gone (a caller's stream destroyed
+    // before the plan): free synchronously then
+    if (cudaFreeAsync(p, s) != cudaSuccess) {
+        cudaGetLastError();
+        cudaFree(p);
+    }
 }
 void debug_fail_alloc_after(int n) {
     std::lock_guard<std::mutex> lk(g_alloc_mu);
