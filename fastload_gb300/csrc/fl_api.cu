@@ -596,6 +596,13 @@ int fl_plan_spmv_host(fl_plan_t p, const double *h_xs, double *h_y, int variant,
         // band while that copy is in flight and takes the light items once
         // the epoch is in.
         const int H0 = B->heavy.H0;
+        if (!B->light_fine_built) {
+            // the light items of this call run after most of the band, on
+            // every warp: cut finer than the device-resident kernel's
+            Bucket *Bm = p->bucket.get();
+            FL_TRY(build_regions_sized(Bm->light, item_nnz_for(Bm->light.nnz), Bm->light_fine, s));
+            Bm->light_fine_built = true;
+        }
         if (!p->side) {
             FL_CUDA(cudaStreamCreateWithFlags(&p->side, cudaStreamNonBlocking));
             FL_CUDA(cudaEventCreateWithFlags(&p->fork, cudaEventDisableTiming));

@@ -328,6 +328,11 @@ int spmv_bucket_f64(const Bucket &B, const double *xs, double *y, int accumulate
     a.err_host = nullptr;
     if (xu) {
         if (!bucket_overlap_ok(B)) return fail(FL_ERR_ARG, "spmv_bucket: overlapped upload does not apply");
+        if (B.light_fine_built && B.light_fine.nitems > 0) {
+            a.items = B.light_fine.item.get();
+            a.regions = B.light_fine.region.get();
+            a.nitems = B.light_fine.nitems;
+        }
         a.x_ready = xu->flag;
         a.x_epoch = xu->epoch;
         a.err_host = xu->err_host;

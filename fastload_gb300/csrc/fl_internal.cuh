@@ -166,6 +166,11 @@ struct Bucket {
     Layout light;
     HeavyBand heavy;
     DevBuf<int> err;            // device status word of the bucket kernel
+    // the light part cut into finer work items (about two per warp of the
+    // GPU for the light part alone) for the overlapped host call, whose
+    // light items run once the band is mostly done; built on first use
+    Regions light_fine;
+    bool light_fine_built = false;
 };
 
 // A storage / right-hand-side form of a plan: its own bucketed split (light
@@ -232,6 +237,9 @@ int build_layout_device(Layout &L, int m, int n, int nnz, const int *sortnnz,
 // sortnnz is non-negative, ascending and sums to nnz.
 int build_steps(Layout &L, int m, int n, int nnz, const int *sortnnz, cudaStream_t s);
 int build_regions(Layout &L, cudaStream_t s);
+// Regions and work items of `item` nonzeros (a multiple of 4) over L's
+// step table, into R.
+int build_regions_sized(const Layout &L, int item, Regions &R, cudaStream_t s);
 // Checks that host-provided per-tile arrays equal the ones the step table
 // implies (so the streaming kernels may derive columns arithmetically).
 int check_tile_meta(const Layout &L, const int *tile_ptr, const int *tile_len,

@@ -801,9 +801,11 @@ int item_nnz_for(long nnz) {
 }
 
 int build_regions(Layout &L, cudaStream_t s) {
-    StepTable &st = L.st;
-    Regions &R = L.regions;
-    const int item = item_nnz_for(L.item_basis > 0 ? L.item_basis : L.nnz);
+    return build_regions_sized(L, item_nnz_for(L.item_basis > 0 ? L.item_basis : L.nnz), L.regions, s);
+}
+
+int build_regions_sized(const Layout &L, int item, Regions &R, cudaStream_t s) {
+    const StepTable &st = L.st;
     int nreg = 2 * st.steps;
     R.nregions = nreg;
     R.nitems = 0;
