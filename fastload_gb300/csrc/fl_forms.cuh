@@ -307,15 +307,21 @@ __device__ __forceinline__ void heavy_unit_ring(const FormArgs<V, Y> &a, int sl,
     // arrays carry past their end; the consumer stops at T.  Every call
     // commits a group (empty past the unit) so the per-thread group count
     // stays in step with k.  This lane's 16-byte pieces are fixed offsets.
-    const char *vsrc = (const char *)(a.hval + 32 * (size_t)T0);
-    const char *csrc = (const char *)(a.hcol16 + 32 * (size_t)T0);
+    static_assert((RING_STAGES & (RING_STAGES - 1)) == 0, "ring slots are taken modulo a power of two");
+    // this lane's pieces: source pointers advanced a stage per issue, slot
+    // offsets fixed
+    const char *vsrc = (const char *)(a.hval + 32 * (size_t)T0) + lane * 16;
+    const char *csrc = (const char *)(a.hcol16 + 32 * (size_t)T0) + lane * 16;
+    unsigned char *lring = ring + lane * 16;
     auto issue = [&](int k) {
         if (k < nst) {
-            unsigned char *slot = ring + (k % RING_STAGES) * SB;
+            unsigned char *slot = lring + (k & (RING_STAGES - 1)) * SB;
 #pragma unroll
             for (int off = 0; off < VB; off += 512)
-                if (off + lane * 16 < VB) cp_async16(slot + off + lane * 16, vsrc + (size_t)k * VB + off + lane * 16);
-            if (lane * 16 < CB) cp_async16(slot + VB + lane * 16, csrc + (size_t)k * CB + lane * 16);
+                if (off + lane * 16 < VB) cp_async16(slot + off, vsrc + off);
+            if (lane * 16 < CB) cp_async16(slot + VB, csrc);
+            vsrc += VB;
+            csrc += CB;
         }
         cp_async_commit();
     };
@@ -335,7 +341,7 @@ __device__ __forceinline__ void heavy_unit_ring(const FormArgs<V, Y> &a, int sl,
     for (int k = 0; k < nst; k++) {
         cp_async_wait<RING_STAGES - 1>();
         __syncwarp();
-        const unsigned char *slot = ring + (k % RING_STAGES) * SB;
+        const unsigned char *slot = ring + (k & (RING_STAGES - 1)) * SB;
         const V *sv = (const V *)slot;
         const uint16_t *sc = (const uint16_t *)(slot + VB);
         const int t0 = k * RING_STEPS;
