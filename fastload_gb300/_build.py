@@ -26,7 +26,7 @@ ORACLE_DIR = os.path.join(ROOT, "oracle")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
-              "--expt-relaxed-constexpr", "-I", INCLUDE]
+              "-Xcompiler", "-fvisibility=hidden", "--expt-relaxed-constexpr", "-I", INCLUDE]
 
 
 def nvcc() -> str:

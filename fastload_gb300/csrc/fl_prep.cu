@@ -902,6 +902,12 @@ static int scan_exclusive_into(const int *in, int *out, long n, int *total, int 
     return FL_SUCCESS;
 }
 
+}  // namespace fl
+
+using namespace fl;
+
+// At global scope: an extern "C" definition inside a namespace does not take
+// the exported visibility of its declaration in fastload.h.
 extern "C" int fl_col_sort_noalloc(int n, int nnz, const int *d_nnzpercol, const int *d_colptr,
                                    const int *d_rowidx, const double *d_val, const double *d_x, int *d_perm,
                                    int *d_sortnnz, int *d_sortrowidx_tmp, double *d_sortval_tmp, double *d_sortx,
@@ -966,5 +972,3 @@ extern "C" int fl_col_sort_noalloc(int n, int nnz, const int *d_nnzpercol, const
     }
     return FL_SUCCESS;
 }
-
-}  // namespace fl

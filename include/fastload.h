@@ -32,6 +32,13 @@
 extern "C" {
 #endif
 
+/* The library is built with hidden visibility: the functions declared here
+ * are its only exports, so its internal C++ symbols (and the static state of
+ * its templates) never bind to another library's in the same process. */
+#if defined(__GNUC__)
+#pragma GCC visibility push(default)
+#endif
+
 #define FL_SUCCESS 0
 #define FL_ERR_ARG (-1)       /* bad argument, malformed or inconsistent input */
 #define FL_ERR_CUDA (-2)      /* CUDA runtime error */
@@ -469,6 +476,10 @@ void fl_debug_fail_alloc_after(int countdown);
  * has arrived, so the kernel's bounded wait for it runs out (about a second)
  * and the call returns FL_ERR_NOT_READY.  For the failure-detection test. */
 void fl_debug_hold_x_upload(int hold);
+
+#if defined(__GNUC__)
+#pragma GCC visibility pop
+#endif
 
 #ifdef __cplusplus
 }

@@ -42,6 +42,23 @@ def test_library_exports_every_declared_symbol(built_lib):
     assert declared <= bound | {"fl_plan_info_get"}, sorted(declared - bound)
 
 
+def test_library_exports_only_the_c_api(built_lib):
+    """Built with hidden visibility: no C function beyond the header's, and no
+    GNU-unique symbol (the static state of a template instantiation, which the
+    dynamic linker shares across every library in the process that defines
+    it)."""
+    from fastload_gb300 import _build
+
+    out = subprocess.run(["nm", "-D", "--defined-only", _build.lib_path()], capture_output=True, text=True,
+                         check=True).stdout
+    rows = [ln.split() for ln in out.splitlines() if ln.strip()]
+    unique = [r[-1] for r in rows if r[-2] == "u"]
+    assert not unique, f"GNU-unique exports: {unique[:5]}"
+    c_funcs = {r[-1] for r in rows if r[-2] == "T" and not r[-1].startswith("_Z")}
+    extra = sorted(c_funcs - declared_symbols())
+    assert not extra, f"exported but not declared in include/: {extra}"
+
+
 def test_library_is_built_for_sm_103a_only(built_lib):
     from fastload_gb300 import _build
 
