@@ -95,6 +95,24 @@ struct Timer {
     }
 };
 
+// On an error return of a host-buffer call, waits for the work the call has
+// already queued on its streams, so that no copy from or into the caller's
+// (possibly pinned) host buffers is still running once the call returns.
+// Disarmed on success: the pipelined call returns with its copies in flight
+// by design.
+struct DrainOnError {
+    cudaStream_t st[4];
+    int n = 0;
+    bool ok = false;
+    void add(cudaStream_t s) {
+        if (n < 4) st[n++] = s;
+    }
+    ~DrainOnError() {
+        if (ok) return;
+        for (int i = 0; i < n; i++) cudaStreamSynchronize(st[i]);
+    }
+};
+
 template <typename T>
 T *host_alloc(size_t count) {
     return (T *)calloc(count ? count : 1, sizeof(T));
@@ -580,6 +598,8 @@ int fl_plan_spmv_host(fl_plan_t p, const double *h_xs, double *h_y, int variant,
     clear_error();
     if (!p || (p->L.n && !h_xs) || (p->L.m && !h_y)) return fail(FL_ERR_ARG, "plan_spmv_host: NULL argument");
     cudaStream_t s = (cudaStream_t)stream;
+    DrainOnError drain;
+    drain.add(s);
     if (p->stage_x.n < (size_t)p->L.n) FL_TRY(p->stage_x.alloc(p->L.n, s));
     if (p->stage_y.n < (size_t)p->L.m) FL_TRY(p->stage_y.alloc(p->L.m, s));
     double *dx = p->stage_x.get();
@@ -608,6 +628,7 @@ int fl_plan_spmv_host(fl_plan_t p, const double *h_xs, double *h_y, int variant,
             FL_CUDA(cudaEventCreateWithFlags(&p->fork, cudaEventDisableTiming));
             FL_CUDA(cudaEventCreateWithFlags(&p->join, cudaEventDisableTiming));
         }
+        drain.add(p->side);
         if (!p->epoch_host) {
             // [0] the epoch word, [1] the kernel's status word (written by the
             // kernel through the mapping only when a wait expires)
@@ -651,6 +672,7 @@ int fl_plan_spmv_host(fl_plan_t p, const double *h_xs, double *h_y, int variant,
         FL_CUDA(cudaStreamSynchronize(s));
         return fail(FL_ERR_NOT_READY, "plan_spmv_host: a bounded device wait expired (0x%x); y is incomplete", h);
     }
+    drain.ok = true;
     return FL_SUCCESS;
 }
 
@@ -668,6 +690,10 @@ int fl_plan_spmv_host_async(fl_plan_t p, const double *h_xs, double *h_y, int va
             FL_CUDA(cudaEventCreateWithFlags(&a.down, cudaEventDisableTiming));
         }
     }
+    DrainOnError drain;
+    drain.add(p->up_s);
+    drain.add(p->comp_s);
+    drain.add(p->down_s);
     fl_plan::AsyncSlot &S = p->slot[p->slot_next];
     // stream-ordered allocations on the upload stream: every later use of
     // the slot (compute, download) is ordered after the upload
@@ -694,6 +720,7 @@ int fl_plan_spmv_host_async(fl_plan_t p, const double *h_xs, double *h_y, int va
     FL_CUDA(cudaStreamWaitEvent(s, S.down, 0));
     S.used = true;
     p->slot_next ^= 1;
+    drain.ok = true;
     return FL_SUCCESS;
 }
 

@@ -209,7 +209,8 @@ int fl_plan_spmv(fl_plan_t plan, const double *d_xs, double *d_y,
                  int accumulate, int variant, void *stream);
 /* Host-buffer SpMV through the plan: copies xs (n doubles) to the device,
  * runs y = A xs and copies y (m doubles) back; synchronous on `stream`.
- * Pinned host buffers give the fastest copies. */
+ * Pinned host buffers give the fastest copies.  On an error return no copy
+ * from h_xs or into h_y is still running. */
 int fl_plan_spmv_host(fl_plan_t plan, const double *h_xs, double *h_y,
                       int variant, void *stream);
 /* Pipelined host-buffer SpMV: enqueues the copy of xs to the device, y = A xs
@@ -222,7 +223,8 @@ int fl_plan_spmv_host(fl_plan_t plan, const double *h_xs, double *h_y,
  * for earlier work on `stream`: h_xs must hold x when the call is made, and
  * may be reused, like h_y read, only after that synchronisation.  Both
  * should be pinned (page-locked) host memory, otherwise the copies are
- * synchronous and nothing overlaps. */
+ * synchronous and nothing overlaps.  On an error return the call has waited
+ * for what it had queued: no copy from h_xs or into h_y is still running. */
 int fl_plan_spmv_host_async(fl_plan_t plan, const double *h_xs, double *h_y,
                             int variant, void *stream);
 int fl_plan_destroy(fl_plan_t plan);
