@@ -267,6 +267,7 @@ int fl_csr_to_csc(double *time_ms, int m, int n, int nnz, const double *csr_val,
     if (!csr_row_ptr || !csc_col_ptr || !nnzpercol || (nnz && (!csr_val || !csr_col_ind || !csc_val || !csc_row_ind)))
         return fail(FL_ERR_ARG, "csr_to_csc: NULL array");
     cudaStream_t s = 0;
+    SyncAtExit drain{s};
     DevBuf<int> rp, ci, cp, cr, npc;
     DevBuf<double> v, cv;
     FL_TRY(upload(rp, csr_row_ptr, (size_t)m + 1, s));
@@ -297,6 +298,7 @@ int fl_col_sort(double *time_ms, int rowA, int colA, int nnz, const int *nnzPerC
         (nnz && (!cscRowIdx || !cscVal || !sortrowidxTmp || !sortvalTmp)) || (colA && x && !sortx))
         return fail(FL_ERR_ARG, "ColSort: NULL array");
     cudaStream_t s = 0;
+    SyncAtExit drain{s};
     DevBuf<int> cnt, cp, cr, perm, snnz, srow;
     DevBuf<double> cv, dx, dxs, sval;
     FL_TRY(upload(cnt, nnzPerCol, colA, s));
@@ -332,6 +334,7 @@ int fl_format_transform(double *time_tran_ms, double *time_class_ms, fl_slide_ma
     if (!matrix || (colA && !sortnnz_tmp) || (nnz && (!sortrowidx_tmp || !sortval_tmp)))
         return fail(FL_ERR_ARG, "formatTransform: NULL argument");
     cudaStream_t s = 0;
+    SyncAtExit drain{s};
     DevBuf<int> snnz, srow;
     DevBuf<double> sval;
     FL_TRY(upload(snnz, sortnnz_tmp, colA, s));
@@ -353,6 +356,7 @@ int fl_fastload_spmv(const fl_slide_matrix *matrix, int nnz, int colA, int rowA,
     if (!matrix || (colA && !x_sorted) || (rowA && !y)) return fail(FL_ERR_ARG, "FastLoad_spmv: NULL argument");
     if (reps < 0) return fail(FL_ERR_ARG, "FastLoad_spmv: reps=%d", reps);
     cudaStream_t s = 0;
+    SyncAtExit drain{s};
     Layout L;
     FL_TRY(upload_layout(L, matrix, rowA, colA, nnz, s));
     // The bucketed split of the uploaded layout when it has a band of dense

@@ -182,6 +182,7 @@ int host_timed(int m, int n, int nnz, const int *ptr, int nptr, const int *idx, 
     if (m < 0 || n < 0 || nnz < 0 || reps < 1 || !ptr || !x || !y || !mean_ms || (nnz && (!idx || !val)))
         return fail(FL_ERR_ARG, "comparator: bad arguments (m=%d n=%d nnz=%d reps=%d)", m, n, nnz, reps);
     const cudaStream_t s = 0;
+    SyncAtExit drain{s};
     DevBuf<int> dp, di;
     DevBuf<double> dv, dx, dy;
     FL_TRY(dp.alloc(nptr, s));
@@ -195,13 +196,16 @@ int host_timed(int m, int n, int nnz, const int *ptr, int nptr, const int *idx, 
         FL_CUDA(cudaMemcpyAsync(dv.get(), val, (size_t)nnz * sizeof(double), cudaMemcpyHostToDevice, s));
     }
     if (n) FL_CUDA(cudaMemcpyAsync(dx.get(), x, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, s));
-    cudaEvent_t a, b;
-    FL_CUDA(cudaEventCreate(&a));
-    FL_CUDA(cudaEventCreate(&b));
     struct Ev {
-        cudaEvent_t a, b;
-        ~Ev() { cudaEventDestroy(a); cudaEventDestroy(b); }
-    } ev{a, b};
+        cudaEvent_t a = nullptr, b = nullptr;
+        ~Ev() {
+            if (a) cudaEventDestroy(a);
+            if (b) cudaEventDestroy(b);
+        }
+    } ev;
+    FL_CUDA(cudaEventCreate(&ev.a));
+    FL_CUDA(cudaEventCreate(&ev.b));
+    const cudaEvent_t a = ev.a, b = ev.b;
     FL_TRY(launch(dp.get(), di.get(), dv.get(), dx.get(), dy.get()));  // untimed: first-call set-up
     double total = 0;
     for (int r = 0; r < reps; r++) {

@@ -69,6 +69,15 @@ struct DevBuf {
     T *get() const { return p; }
 };
 
+// Synchronises a stream when it goes out of scope.  Declared before a
+// synchronous host-buffer call's device buffers, it makes the call return,
+// on every path, only after the copies it queued from or into the caller's
+// host buffers (possibly pinned) have finished.
+struct SyncAtExit {
+    cudaStream_t s;
+    ~SyncAtExit() { cudaStreamSynchronize(s); }
+};
+
 // ---------------------------------------------------------------- layout --
 // Device-resident FastLoad layout of one matrix.  The tile-ordered value and
 // row streams are the reference's sortval/sortrowidx (bit-identical); the
