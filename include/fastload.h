@@ -34,7 +34,14 @@ extern "C" {
 
 /* The library is built with hidden visibility: the functions declared here
  * are its only exports, so its internal C++ symbols (and the static state of
- * its templates) never bind to another library's in the same process. */
+ * its templates) never bind to another library's in the same process.  The
+ * opaque handle types are declared before the default-visibility region, so
+ * their members stay internal too. */
+struct fl_plan;
+struct fl_mtx;
+struct fl_cusparse;
+struct fl_batch;
+struct fl_mlp;
 #if defined(__GNUC__)
 #pragma GCC visibility push(default)
 #endif

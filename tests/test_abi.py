@@ -57,6 +57,10 @@ def test_library_exports_only_the_c_api(built_lib):
     c_funcs = {r[-1] for r in rows if r[-2] == "T" and not r[-1].startswith("_Z")}
     extra = sorted(c_funcs - declared_symbols())
     assert not extra, f"exported but not declared in include/: {extra}"
+    # C++ exports: only standard-library template instances (default
+    # visibility in libstdc++'s own headers), none of the library's types
+    own = [r[-1] for r in rows if r[-1].startswith("_Z") and not r[-1].startswith(("_ZNSt", "_ZSt", "_ZNKSt"))]
+    assert not own, f"library C++ symbols exported: {own[:5]}"
 
 
 def test_library_is_built_for_sm_103a_only(built_lib):
