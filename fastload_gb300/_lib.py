@@ -167,6 +167,15 @@ class FastLoadError(RuntimeError):
         self.code = code
 
 
+class FastLoadArgumentError(FastLoadError, ValueError):
+    """An argument the Python layer rejected before calling the library (a
+    tensor or array of the wrong device, type, layout or length, which the
+    C ABI's plain pointers could not detect).  Code FL_ERR_ARG."""
+
+    def __init__(self, msg: str):
+        super().__init__(-1, msg)
+
+
 def check(rc: int) -> None:
     if rc != 0:
         msg = load().fl_last_error()

@@ -7,7 +7,7 @@ import ctypes as C
 import numpy as np
 
 from ._lib import check, load
-from .plan import VALUES_F32, Plan, _dev, _stream_handle, _torch
+from .plan import VALUES_F32, Plan, _dev, _need_cuda, _stream_handle, _torch
 
 
 class Batch:
@@ -30,25 +30,33 @@ class Batch:
     def permute_x(self, x, stream=None):
         torch = _torch()
         x = _dev(x, torch.float64)
+        _need_cuda(x, torch.float64, self.n, "batch permute_x x")
         xs = torch.empty(self.n, dtype=torch.float64 if self.value_type == 0 else torch.float32, device="cuda")
         check(load().fl_batch_permute_x(self._h, C.c_void_p(x.data_ptr()), C.c_void_p(xs.data_ptr()),
                                         _stream_handle(stream)))
         return xs
 
-    def _y(self, y):
+    def _y(self, xs, y):
+        """Checks xs (float64 for FP64 values, else float32; n stacked
+        columns) and y (float32 when y_f32, else float64; m stacked rows),
+        allocating y when it is None."""
         torch = _torch()
+        _need_cuda(xs, torch.float64 if self.value_type == 0 else torch.float32, self.n, "batch xs")
+        ydt = torch.float32 if self.y_f32 else torch.float64
         if y is None:
-            y = torch.empty(self.m, dtype=torch.float32 if self.y_f32 else torch.float64, device="cuda")
+            y = torch.empty(self.m, dtype=ydt, device="cuda")
+        else:
+            _need_cuda(y, ydt, self.m, "batch y")
         return y
 
     def spmv(self, xs, y=None, stream=None):
-        y = self._y(y)
+        y = self._y(xs, y)
         check(load().fl_batch_spmv(self._h, C.c_void_p(xs.data_ptr()), C.c_void_p(y.data_ptr()),
                                    _stream_handle(stream)))
         return y
 
     def spmv_graph(self, xs, y=None, stream=None):
-        y = self._y(y)
+        y = self._y(xs, y)
         check(load().fl_batch_spmv_graph(self._h, C.c_void_p(xs.data_ptr()), C.c_void_p(y.data_ptr()),
                                          _stream_handle(stream)))
         return y

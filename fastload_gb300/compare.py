@@ -7,6 +7,7 @@ from __future__ import annotations
 import ctypes as C
 
 from ._lib import check, load
+from .plan import _need_cuda
 
 
 def _torch():
@@ -23,10 +24,13 @@ def _stream(stream):
 def csc_spmv_naive(m, colptr, rowidx, val, x, y=None, accumulate=False, stream=None):
     """y = A x (original column order) with the naive CSC kernel."""
     torch = _torch()
+    n = colptr.numel() - 1
+    _need_cuda(x, torch.float64, n, "csc_spmv_naive x")
     if y is None:
         y = torch.empty(m, dtype=torch.float64, device="cuda")
         accumulate = False
-    n = colptr.numel() - 1
+    else:
+        _need_cuda(y, torch.float64, m, "csc_spmv_naive y")
     check(load().fl_csc_spmv_naive(m, n, rowidx.numel(), C.c_void_p(colptr.data_ptr()),
                                    C.c_void_p(rowidx.data_ptr()), C.c_void_p(val.data_ptr()),
                                    C.c_void_p(x.data_ptr()), C.c_void_p(y.data_ptr()), int(accumulate),
@@ -48,8 +52,11 @@ class CuSparse:
 
     def spmv(self, x, y=None, stream=None):
         torch = _torch()
+        _need_cuda(x, torch.float64, self.n, "cusparse spmv x")
         if y is None:
             y = torch.empty(self.m, dtype=torch.float64, device="cuda")
+        else:
+            _need_cuda(y, torch.float64, self.m, "cusparse spmv y")
         check(load().fl_cusparse_spmv(self._h, C.c_void_p(x.data_ptr()), C.c_void_p(y.data_ptr()),
                                       _stream(stream)))
         return y

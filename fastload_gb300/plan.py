@@ -11,7 +11,7 @@ import struct
 
 import numpy as np
 
-from ._lib import FormInfoC, PlanInfoC, PlanOptsC, SlideMatrixC, check, load
+from ._lib import FastLoadArgumentError, FormInfoC, PlanInfoC, PlanOptsC, SlideMatrixC, check, load
 from .host import SlideMatrix
 
 KERNEL_AUTO = 0
@@ -100,6 +100,27 @@ def _stream_handle(stream) -> C.c_void_p:
     return C.c_void_p(s.cuda_stream)
 
 
+def _need_cuda(t, dtype, count: int, what: str) -> None:
+    """The kernels index plain device pointers: t must be a contiguous CUDA
+    tensor of dtype holding at least count elements."""
+    if not (getattr(t, "is_cuda", False) and t.dtype == dtype and t.is_contiguous()):
+        raise FastLoadArgumentError(
+            f"{what}: needs a contiguous CUDA tensor of {dtype}, got {type(t).__name__} "
+            f"{getattr(t, 'dtype', '')} on {getattr(t, 'device', 'host')}")
+    if t.numel() < count:
+        raise FastLoadArgumentError(f"{what}: needs at least {count} elements, got {t.numel()}")
+
+
+def _need_host(a, count: int, what: str) -> None:
+    """A host array the library copies from or into: C-contiguous float64
+    numpy with at least count elements."""
+    if not (isinstance(a, np.ndarray) and a.dtype == np.float64 and a.flags.c_contiguous):
+        raise FastLoadArgumentError(f"{what}: needs a C-contiguous float64 numpy array, got "
+                                    f"{type(a).__name__} {getattr(a, 'dtype', '')}")
+    if a.size < count:
+        raise FastLoadArgumentError(f"{what}: needs at least {count} elements, got {a.size}")
+
+
 def _dev(a, dtype):
     """A contiguous CUDA tensor of dtype (uploads numpy input)."""
     torch = _torch()
@@ -115,6 +136,7 @@ class Plan:
     def __init__(self, handle: C.c_void_p, keep=None):
         self._h = handle
         self._keep = keep
+        self._form_kinds = {}  # form id -> (value type, y is FP32)
         self.info = self._info()
         self.m, self.n, self.nnz = self.info["m"], self.info["n"], self.info["nnz"]
 
@@ -191,7 +213,10 @@ class Plan:
     # -- compute -------------------------------------------------------------
     def permute_x(self, x, out=None, stream=None):
         torch = _torch()
+        if out is not None:
+            _need_cuda(out, torch.float64, self.n, "permute_x out")
         x = _dev(x, torch.float64)
+        _need_cuda(x, torch.float64, self.n, "permute_x x")
         xs = out if out is not None else torch.empty(self.n, dtype=torch.float64, device="cuda")
         check(load().fl_plan_permute_x(self._h, C.c_void_p(x.data_ptr()), C.c_void_p(xs.data_ptr()),
                                        _stream_handle(stream)))
@@ -200,9 +225,12 @@ class Plan:
     def spmv(self, xs, y=None, accumulate: bool = False, kernel: int = KERNEL_AUTO, stream=None):
         """y = A xs (or y += A xs); xs in sorted column order (permute_x)."""
         torch = _torch()
+        _need_cuda(xs, torch.float64, self.n, "spmv xs")
         if y is None:
             y = torch.empty(self.m, dtype=torch.float64, device="cuda")
             accumulate = False
+        else:
+            _need_cuda(y, torch.float64, self.m, "spmv y")
         check(load().fl_plan_spmv(self._h, C.c_void_p(xs.data_ptr()), C.c_void_p(y.data_ptr()), int(accumulate),
                                   int(kernel), _stream_handle(stream)))
         return y
@@ -210,8 +238,11 @@ class Plan:
     def spmv_host(self, xs: np.ndarray, y: np.ndarray | None = None, kernel: int = KERNEL_AUTO, stream=None):
         """Host buffers in and out: H2D of xs, SpMV, D2H of y (synchronous)."""
         xs = np.ascontiguousarray(xs, dtype=np.float64)
+        _need_host(xs, self.n, "spmv_host xs")
         if y is None:
             y = np.empty(self.m, np.float64)
+        else:
+            _need_host(y, self.m, "spmv_host y")
         check(load().fl_plan_spmv_host(self._h, C.c_void_p(xs.ctypes.data), C.c_void_p(y.ctypes.data),
                                        int(kernel), _stream_handle(stream)))
         return y
@@ -225,10 +256,8 @@ class Plan:
         must be C-contiguous float64 arrays that stay alive, unmodified (xs)
         and unread (y) until then; pinned memory (torch pin_memory) lets the
         copies overlap."""
-        if xs.dtype != np.float64 or y.dtype != np.float64 or not xs.flags.c_contiguous or not y.flags.c_contiguous:
-            raise ValueError("spmv_host_async needs C-contiguous float64 arrays")
-        if xs.size < self.n or y.size < self.m:
-            raise ValueError("spmv_host_async: xs needs n and y m elements")
+        _need_host(xs, self.n, "spmv_host_async xs")
+        _need_host(y, self.m, "spmv_host_async y")
         check(load().fl_plan_spmv_host_async(self._h, C.c_void_p(xs.ctypes.data), C.c_void_p(y.ctypes.data),
                                              int(kernel), _stream_handle(stream)))
         return y
@@ -239,7 +268,17 @@ class Plan:
         heavy band; returns its id for spmv_form."""
         fid = C.c_int(-1)
         check(load().fl_plan_add_form(self._h, int(value_type), int(heavy_band), int(y_f32), C.byref(fid)))
+        self._form_kinds[fid.value] = (int(value_type), bool(y_f32))
         return fid.value
+
+    def _kinds(self, form_id: int) -> tuple[int, bool]:
+        """(value type, y is FP32) of a form, from the library on first use
+        (forms of a loaded plan file)."""
+        k = self._form_kinds.get(form_id)
+        if k is None:
+            i = self.form_info(form_id)
+            k = self._form_kinds[form_id] = (int(i["value_type"]), bool(i["y_f32"]))
+        return k
 
     def add_tuned_form(self, value_type: int = VALUES_F32, y_f32: bool = False, model=None) -> tuple[int, str]:
         """Adds a form whose heavy band the learned tuner picks for this
@@ -260,17 +299,30 @@ class Plan:
         when to_f32."""
         torch = _torch()
         x = _dev(x, torch.float64).reshape(-1)
+        _need_cuda(x, torch.float64, self.n * max(int(k), 0), "permute_x_k x")
         xs = torch.empty(self.n * k, dtype=torch.float32 if to_f32 else torch.float64, device="cuda")
         check(load().fl_plan_permute_x_k(self._h, int(k), int(to_f32), C.c_void_p(x.data_ptr()),
                                          C.c_void_p(xs.data_ptr()), _stream_handle(stream)))
         return xs
 
-    def spmv_form(self, form_id: int, xs, y=None, k: int = 1, accumulate: bool = False, y_f32: bool = False,
+    def spmv_form(self, form_id: int, xs, y=None, k: int = 1, accumulate: bool = False, y_f32: bool | None = None,
                   stream=None):
+        """y = A xs through a form: xs (n*k, sorted column order, rows of k
+        interleaved) is float64 for an FP64 form and float32 otherwise
+        (permute_x_k); y (m*k) is float32 when the form accumulates in FP32,
+        else float64.  y_f32, when given, must agree with the form."""
         torch = _torch()
+        vtype, form_y32 = self._kinds(int(form_id))
+        if y_f32 is not None and bool(y_f32) != form_y32:
+            raise FastLoadArgumentError(f"spmv_form: form {form_id} has {'an FP32' if form_y32 else 'an FP64'} y")
+        kk = max(int(k), 0)
+        _need_cuda(xs, torch.float64 if vtype == VALUES_F64 else torch.float32, self.n * kk, "spmv_form xs")
+        ydt = torch.float32 if form_y32 else torch.float64
         if y is None:
-            y = torch.empty(self.m * k, dtype=torch.float32 if y_f32 else torch.float64, device="cuda")
+            y = torch.empty(self.m * k, dtype=ydt, device="cuda")
             accumulate = False
+        else:
+            _need_cuda(y, ydt, self.m * kk, "spmv_form y")
         check(load().fl_plan_spmv_form(self._h, int(form_id), int(k), C.c_void_p(xs.data_ptr()),
                                        C.c_void_p(y.data_ptr()), int(accumulate), _stream_handle(stream)))
         return y
