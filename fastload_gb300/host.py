@@ -14,7 +14,7 @@ from dataclasses import dataclass
 
 import numpy as np
 
-from ._lib import FastLoadError, SlideMatrixC, check, load
+from ._lib import FastLoadArgumentError, FastLoadError, SlideMatrixC, check, load
 
 __all__ = ["SlideMatrix", "csr_to_csc", "ColSort", "formatTransform", "FastLoad_spmv", "FastLoadError"]
 
@@ -139,11 +139,19 @@ def FastLoad_spmv(matrix: SlideMatrix, nnz: int, colA: int, rowA: int, x_sorted,
     """y = A x on the GPU from a host slide_matrix.  Returns (y, ms_per_spmv,
     mismatches) where mismatches counts |y_golden - y| > 0.01|y| (0 when no
     golden is given)."""
-    lib = load()
     xs = _f64(x_sorted)
     if xs.size < colA:
         raise FastLoadError(-1, "FastLoad_spmv: x_sorted shorter than colA")
     yg = None if y_golden is None else _f64(y_golden)
+    if yg is not None and yg.size < rowA:
+        raise FastLoadArgumentError(f"FastLoad_spmv: y_golden has {yg.size} entries, rowA={rowA}")
+    # the library copies these many entries of each array to the device
+    T = int(matrix.tilenum)
+    need = {"sortval": nnz, "sortrowidx": nnz, "tile_ptr": T + 1, "tile_len": T, "tile_colidx": T}
+    short = [f"{k} ({np.size(getattr(matrix, k))} < {v})" for k, v in need.items() if np.size(getattr(matrix, k)) < v]
+    if short:
+        raise FastLoadArgumentError("FastLoad_spmv: slide_matrix arrays shorter than tilenum/nnz: " + ", ".join(short))
+    lib = load()
     y = np.empty(rowA, np.float64)
     cm, keep = matrix.to_c()
     ms = C.c_double(0)

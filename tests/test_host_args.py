@@ -72,3 +72,18 @@ def test_batch_and_comparators(no_library):
     assert "CUDA tensor" in rejects(lambda: cs.spmv(torch.zeros(5, dtype=torch.float64)))
     cp = torch.zeros(6, dtype=torch.int32)
     assert "CUDA tensor" in rejects(lambda: compare.csc_spmv_naive(6, cp, cp, cp, torch.zeros(5)))
+
+
+def test_fastload_spmv_checks_the_slide_matrix(monkeypatch):
+    from fastload_gb300 import host
+
+    monkeypatch.setattr(host, "load", lambda: (_ for _ in ()).throw(AssertionError("the library was called")))
+    z = np.zeros
+    sm = host.SlideMatrix(sortval=z(3), sortrowidx=z(3, np.int32), tile_ptr=z(2, np.int32), tile_len=z(2, np.int32),
+                          tile_colidx=z(2, np.int32), tile_tall=z(2, np.int32), tile_format=z(2, np.int32),
+                          countrow=z(3, np.int32), segmentoffset=z(1, np.int32), sortrowindex=z(3, np.int32),
+                          tilenum=2, segsum=0)
+    assert "tile_ptr (2 < 3)" in rejects(lambda: host.FastLoad_spmv(sm, 3, 2, 4, z(2)))
+    sm.tile_ptr = z(3, np.int32)
+    assert "sortval (3 < 5)" in rejects(lambda: host.FastLoad_spmv(sm, 5, 2, 4, z(2)))
+    assert "y_golden" in rejects(lambda: host.FastLoad_spmv(sm, 3, 2, 4, z(2), y_golden=z(3)))
