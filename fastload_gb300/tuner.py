@@ -31,7 +31,7 @@ import time
 
 import numpy as np
 
-from ._lib import check, load
+from ._lib import FastLoadArgumentError, check, load
 
 FAMILIES = ("uniform", "zipf", "banded", "blockdiag", "rowskew")
 VARIANTS = ("none", "2048", "8192", "max", "all", "auto")
@@ -202,24 +202,35 @@ class Network:
         return p
 
     def set_params(self, p) -> None:
-        p = np.ascontiguousarray(p, np.float32)
+        p = np.ascontiguousarray(p, np.float32).reshape(-1)
+        if p.size != self.num_params:
+            raise FastLoadArgumentError(f"set_params: {p.size} values for a network of {self.num_params}")
         check(load().fl_mlp_set_params(self._h, p.ctypes.data_as(C.POINTER(C.c_float))))
 
     @staticmethod
     def _fp(a):
         return np.ascontiguousarray(a, np.float32).ctypes.data_as(C.POINTER(C.c_float))
 
+    @staticmethod
+    def _mat(a, cols: int, what: str, rows: int | None = None) -> np.ndarray:
+        """a as a C-contiguous float32 (rows, cols) matrix: the library reads
+        rows * cols values from it."""
+        a = np.ascontiguousarray(a, np.float32)
+        if a.ndim != 2 or a.shape[1] != cols or (rows is not None and a.shape[0] != rows):
+            raise FastLoadArgumentError(f"{what}: shape {a.shape}, expected ({'rows' if rows is None else rows}, {cols})")
+        return a
+
     def forward_raw(self, X) -> np.ndarray:
         """Network outputs for already-scaled features."""
-        X = np.ascontiguousarray(X, np.float32)
+        X = self._mat(X, self.shape[0], "forward X")
         Y = np.empty((X.shape[0], self.shape[3]), np.float32)
         check(load().fl_mlp_forward(self._h, self._fp(X), X.shape[0], Y.ctypes.data_as(C.POINTER(C.c_float))))
         return Y
 
     def grad_raw(self, X, Tg, M=None):
-        X = np.ascontiguousarray(X, np.float32)
-        Tg = np.ascontiguousarray(Tg, np.float32)
-        Mk = None if M is None else np.ascontiguousarray(M, np.float32)
+        X = self._mat(X, self.shape[0], "grad X")
+        Tg = self._mat(Tg, self.shape[3], "grad targets", X.shape[0])
+        Mk = None if M is None else self._mat(M, self.shape[3], "grad mask", X.shape[0])
         loss = np.zeros(1, np.float32)
         g = np.empty(self.num_params, np.float32)
         check(load().fl_mlp_grad(self._h, self._fp(X), self._fp(Tg), None if Mk is None else self._fp(Mk),
@@ -229,13 +240,11 @@ class Network:
 
     def fit(self, X, times, epochs=3000, lr=3e-3) -> np.ndarray:
         """Trains on features X and measured times (ms per variant)."""
-        X = np.asarray(X, np.float32)
+        X = self._mat(X, self.shape[0], "fit X")
+        Tg = self._mat(targets(times), self.shape[3], "fit times", X.shape[0])
         self.mu = X.mean(0)
         self.sd = X.std(0) + 1e-6
-        Xn = (X - self.mu) / self.sd
-        Tg = targets(times)
-        Xn = np.ascontiguousarray(Xn, np.float32)
-        Tg = np.ascontiguousarray(Tg, np.float32)
+        Xn = np.ascontiguousarray((X - self.mu) / self.sd, np.float32)
         losses = np.empty(epochs, np.float32)
         check(load().fl_mlp_train(self._h, self._fp(Xn), self._fp(Tg), None, Xn.shape[0], epochs, C.c_float(lr),
                                   losses.ctypes.data_as(C.POINTER(C.c_float))))

@@ -87,3 +87,18 @@ def test_fastload_spmv_checks_the_slide_matrix(monkeypatch):
     sm.tile_ptr = z(3, np.int32)
     assert "sortval (3 < 5)" in rejects(lambda: host.FastLoad_spmv(sm, 5, 2, 4, z(2)))
     assert "y_golden" in rejects(lambda: host.FastLoad_spmv(sm, 3, 2, 4, z(2), y_golden=z(3)))
+
+
+def test_tuner_network_checks_shapes(monkeypatch):
+    from fastload_gb300 import tuner
+
+    net = tuner.Network.__new__(tuner.Network)
+    net._h, net.shape = None, (24, 64, 64, 6)
+    monkeypatch.setattr(tuner, "load", lambda: (_ for _ in ()).throw(AssertionError("the library was called")))
+    assert "expected (rows, 24)" in rejects(lambda: net.forward_raw(np.zeros((3, 23))))
+    assert "expected (rows, 24)" in rejects(lambda: net.forward_raw(np.zeros(24)))
+    assert "expected (3, 6)" in rejects(lambda: net.grad_raw(np.zeros((3, 24)), np.zeros((2, 6))))
+    assert "expected (3, 6)" in rejects(lambda: net.grad_raw(np.zeros((3, 24)), np.zeros((3, 6)), np.zeros((3, 5))))
+    assert "expected (4, 6)" in rejects(lambda: net.fit(np.zeros((4, 24)), np.ones((4, 5)), epochs=1))
+    monkeypatch.setattr(tuner.Network, "num_params", property(lambda self: 10))
+    assert "9 values" in rejects(lambda: net.set_params(np.zeros(9)))
