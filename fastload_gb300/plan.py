@@ -148,7 +148,15 @@ class Plan:
         column pointer).  heavy_band: -1 no bucketed form, 0 automatic, > 0
         width of the heavy band in columns."""
         torch = _torch()
+        if m < 0 or n < 0:
+            raise FastLoadArgumentError(f"plan create: negative size (m={m} n={n})")
         p, i, v = _dev(ptr, torch.int32), _dev(idx, torch.int32), _dev(val, torch.float64)
+        # the library validates the arrays' contents on the device, reading
+        # (m or n) + 1 pointers and nnz values
+        npt = (m if input_format == INPUT_CSR else n) + 1
+        if p.numel() < npt or v.numel() < i.numel():
+            raise FastLoadArgumentError(f"plan create: {p.numel()} pointers (need {npt}), {v.numel()} values for "
+                                        f"{i.numel()} indices")
         o = PlanOptsC(int(with_reference_arrays), int(heavy_band))
         h = C.c_void_p()
         check(load().fl_plan_create(C.byref(h), int(input_format), m, n, int(i.numel()), C.c_void_p(p.data_ptr()),

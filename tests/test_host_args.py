@@ -102,3 +102,7 @@ def test_tuner_network_checks_shapes(monkeypatch):
     assert "expected (4, 6)" in rejects(lambda: net.fit(np.zeros((4, 24)), np.ones((4, 5)), epochs=1))
     monkeypatch.setattr(tuner.Network, "num_params", property(lambda self: 10))
     assert "9 values" in rejects(lambda: net.set_params(np.zeros(9)))
+
+
+def test_plan_create_rejects_negative_sizes(no_library):
+    assert "negative size" in rejects(lambda: fl.Plan.from_csr(-1, 3, np.zeros(1), np.zeros(0), np.zeros(0)))
