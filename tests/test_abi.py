@@ -115,3 +115,23 @@ def test_tile_destroy_accepts_empty(built_lib):
     m = _lib.SlideMatrixC()
     built_lib.fl_tile_destroy(C.byref(m))
     built_lib.fl_tile_destroy(None)
+
+
+def test_dropin_program_links_against_the_library(built_lib, tmp_path):
+    """tests/dropin/main_dropin.cpp (the reference main.cu's call sequence on
+    fastload_compat.h) compiles with g++ and links: every fl_ symbol it needs
+    is exported.  Running it needs the GPU (test_gpu_parity.py)."""
+    import shutil
+
+    from fastload_gb300 import _build
+
+    if not shutil.which("g++"):
+        pytest.skip("no g++")
+    exe = str(tmp_path / "dropin")
+    subprocess.run(["g++", "-O2", "-std=c++17", "-I", os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "dropin", "main_dropin.cpp"), "-o", exe,
+                    "-L", _build.LIBDIR, "-lfastload_gb300", f"-Wl,-rpath,{_build.LIBDIR}"], check=True)
+    out = subprocess.run(["nm", "-D", "--undefined-only", exe], capture_output=True, text=True, check=True).stdout
+    needed = {ln.split()[-1] for ln in out.splitlines() if ln.split() and ln.split()[-1].startswith("fl_")}
+    assert needed, "the drop-in program calls no library function"
+    assert needed <= exported_symbols(_build.lib_path())
