@@ -627,11 +627,9 @@ int fl_plan_spmv_host(fl_plan_t p, const double *h_xs, double *h_y, int variant,
             FL_TRY(build_regions_sized(Bm->light, item_nnz_for(Bm->light.nnz), Bm->light_fine, s));
             Bm->light_fine_built = true;
         }
-        if (!p->side) {
-            FL_CUDA(cudaStreamCreateWithFlags(&p->side, cudaStreamNonBlocking));
-            FL_CUDA(cudaEventCreateWithFlags(&p->fork, cudaEventDisableTiming));
-            FL_CUDA(cudaEventCreateWithFlags(&p->join, cudaEventDisableTiming));
-        }
+        if (!p->side) FL_CUDA(cudaStreamCreateWithFlags(&p->side, cudaStreamNonBlocking));
+        if (!p->fork) FL_CUDA(cudaEventCreateWithFlags(&p->fork, cudaEventDisableTiming));
+        if (!p->join) FL_CUDA(cudaEventCreateWithFlags(&p->join, cudaEventDisableTiming));
         drain.add(p->side);
         if (!p->epoch_host) {
             // [0] the epoch word, [1] the kernel's status word (written by the
@@ -684,16 +682,13 @@ int fl_plan_spmv_host_async(fl_plan_t p, const double *h_xs, double *h_y, int va
     clear_error();
     if (!p || (p->L.n && !h_xs) || (p->L.m && !h_y)) return fail(FL_ERR_ARG, "plan_spmv_host_async: NULL argument");
     cudaStream_t s = (cudaStream_t)stream;
-    if (!p->up_s) {
-        FL_CUDA(cudaStreamCreateWithFlags(&p->up_s, cudaStreamNonBlocking));
-        FL_CUDA(cudaStreamCreateWithFlags(&p->comp_s, cudaStreamNonBlocking));
-        FL_CUDA(cudaStreamCreateWithFlags(&p->down_s, cudaStreamNonBlocking));
-        for (fl_plan::AsyncSlot &a : p->slot) {
-            FL_CUDA(cudaEventCreateWithFlags(&a.up, cudaEventDisableTiming));
-            FL_CUDA(cudaEventCreateWithFlags(&a.kdone, cudaEventDisableTiming));
-            FL_CUDA(cudaEventCreateWithFlags(&a.down, cudaEventDisableTiming));
-        }
-    }
+    // each handle on its own, so a call after a failed creation makes only
+    // what is still missing
+    for (cudaStream_t *st : {&p->up_s, &p->comp_s, &p->down_s})
+        if (!*st) FL_CUDA(cudaStreamCreateWithFlags(st, cudaStreamNonBlocking));
+    for (fl_plan::AsyncSlot &a : p->slot)
+        for (cudaEvent_t *ev : {&a.up, &a.kdone, &a.down})
+            if (!*ev) FL_CUDA(cudaEventCreateWithFlags(ev, cudaEventDisableTiming));
     DrainOnError drain;
     drain.add(p->up_s);
     drain.add(p->comp_s);
