@@ -18,13 +18,11 @@
 namespace fl {
 
 // ------------------------------------------------------------- errors ----
+// the message of the calling thread's last failure (the code is the
+// call's return value)
 static thread_local std::string g_last_error;
-static thread_local int g_last_code = 0;
 
-void set_error(int code, const std::string &msg) {
-    g_last_code = code;
-    g_last_error = msg;
-}
+void set_error(int, const std::string &msg) { g_last_error = msg; }
 int fail(int code, const char *fmt, ...) {
     char buf[1024];
     va_list ap;
@@ -34,10 +32,7 @@ int fail(int code, const char *fmt, ...) {
     set_error(code, buf);
     return code;
 }
-void clear_error() {
-    g_last_code = 0;
-    g_last_error.clear();
-}
+void clear_error() { g_last_error.clear(); }
 const char *last_error_cstr() { return g_last_error.c_str(); }
 
 // ---------------------------------------------------------- allocation ---
