@@ -140,10 +140,31 @@ class ClockSampler:
                 "samples": len(rows)}
 
 
-def make_workload(n=N_COLS):
-    from fastload_gb300 import gen
+def _gen():
+    """fastload_gb300/gen.py (numpy only), loaded by path: importing the
+    package would load the CUDA library, which the CPU reference arm must
+    not map."""
+    import importlib.util
 
-    return gen.zipf_columns(n, 1.8, 50000, seed=SEED)
+    mod = sys.modules.get("fastload_gb300.gen")
+    if mod is not None:
+        return mod
+    spec = importlib.util.spec_from_file_location("fastload_gb300_gen", os.path.join(ROOT, "fastload_gb300", "gen.py"))
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules[spec.name] = mod  # dataclasses look their module up while the class is made
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def make_workload(n=N_COLS):
+    return _gen().zipf_columns(n, 1.8, 50000, seed=SEED)
+
+
+def bench_config(c, world):
+    """The workload description both arms print (identical dicts)."""
+    return {"workload": workload_name(c.n), "m": c.m, "n": c.n, "nnz": c.nnz, "seed": SEED,
+            "values": "f64", "l2": "inputs larger than L2: matrix streams %.0f MB vs 129 MB L2" % (c.nnz * 12 / 1e6),
+            "parallelism": f"replicas x{world}"}
 
 
 def workload_name(n):
@@ -210,7 +231,7 @@ def run_reference(args, rank, world):
     line = {"impl": "reference", "metric": METRIC, "value": gbs, "unit": "GB/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": DATA,
-            "config": {"workload": workload_name(c.n), "n": c.n, "nnz": c.nnz, "seed": SEED},
+            "config": bench_config(c, world),
             "cpu_baseline": {"value": gbs, "unit": "GB/s", "cores": used, "kind": "port",
                              "sample": f"{args.steps} steps, each 1/{nsamp} of the tiles in turn, FastLoad_cpu "
                                        f"tile loop on {used} OpenMP threads with atomic y updates"},
@@ -273,9 +294,14 @@ def measure_forms(fl, peak, reps=30):
         with fl.Plan.from_csc(c.m, c.n, c.colptr, c.rowidx, c.val) as p:
             xs = p.permute_x(torch.from_numpy(c.x).cuda())
             y = torch.empty(c.m, dtype=torch.float64, device="cuda")
-            t = _time_ms(lambda: p.spmv(xs, y, kernel=fl.KERNEL_STREAM2), reps, flush)
+            # the plain FP64 kernel the forms are compared with: the plan's
+            # default (FL_KERNEL_AUTO), the drop-in FastLoad_spmv path
+            t = _time_ms(lambda: p.spmv(xs, y, kernel=fl.KERNEL_AUTO), reps, flush)
             plain = entry(c, t, 1, 8, 8, y.cpu().numpy(), ref[1])
-            out[f"{cname}_plain_fp64_stream_k1"] = plain
+            out[f"{cname}_plain_fp64_auto_k1"] = plain
+            # context: the pure FastLoad tile stream (one atomic per run)
+            t = _time_ms(lambda: p.spmv(xs, y, kernel=fl.KERNEL_STREAM2), reps, flush)
+            out[f"{cname}_fp64_stream_k1"] = entry(c, t, 1, 8, 8, y.cpu().numpy(), ref[1], plain["gflops"])
             for bname, band in bands:
                 for fname, vt, sv in forms:
                     fid = p.add_form(vt, band)
@@ -298,7 +324,8 @@ def measure_batch(fl, peak, reps=10):
     [1e3, 2e5], mean degree U[4, 32], half Poisson and half Zipf(1.5) column
     degrees), FP32 values with FP32 accumulation, one persistent launch,
     direct and replayed from a captured CUDA graph; against the plain FP64
-    streaming kernel launched once per matrix on the same inputs."""
+    kernel (each plan's default, FL_KERNEL_AUTO) launched once per matrix on
+    the same inputs."""
     import torch
 
     import oracle
@@ -307,7 +334,7 @@ def measure_batch(fl, peak, reps=10):
     mats = gen.batch(256, seed=3, dtype=np.float64)
     flush = torch.empty(64 << 20, dtype=torch.float32, device="cuda")
     t0 = time.perf_counter()
-    plans = [fl.Plan.from_csc(c.m, c.n, c.colptr, c.rowidx, c.val, heavy_band=-1) for c in mats]
+    plans = [fl.Plan.from_csc(c.m, c.n, c.colptr, c.rowidx, c.val) for c in mats]
     prep = time.perf_counter() - t0
     nnz = sum(c.nnz for c in mats)
     M, N = sum(c.m for c in mats), sum(c.n for c in mats)
@@ -319,7 +346,7 @@ def measure_batch(fl, peak, reps=10):
 
     def plain():
         for p, xs_, y_ in zip(plans, xs64, ys64):
-            p.spmv(xs_, y_, kernel=fl.KERNEL_STREAM2)
+            p.spmv(xs_, y_, kernel=fl.KERNEL_AUTO)
 
     t_plain = _time_ms(plain, reps, flush)
     out["plain_fp64_per_matrix"] = {"ms": t_plain, "gflops": 2.0 * nnz / (t_plain * 1e-3) / 1e9, "launches": len(mats)}
@@ -468,16 +495,22 @@ def run_gpu(args, rank, world):
         plan.spmv(xs, y, kernel=kernel)
 
     launches_per_step = plan.info["spmv_launches"]
-    for _ in range(max(args.warmup, 3)):
-        step()
-    torch.cuda.synchronize()
     K = args.steps
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     kstart, kend = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
     with ClockSampler(dev) as clk:
+        # warm-up inside the sampled region, right before the timed steps
+        for _ in range(max(args.warmup, 3)):
+            step()
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        # A device sleep (about a millisecond) ahead of the start event lets
+        # the host enqueue the first steps before the event fires, so the
+        # K steps run back to back on the device from the start event on and
+        # a short run (K = 20) does not carry the host's first-launch latency.
+        torch.cuda._sleep(2_000_000)
         wall0 = time.time()
         start.record(stream)
         for i in range(K):
@@ -536,7 +569,10 @@ def run_gpu(args, rank, world):
     hx_t = [xs_host.clone().pin_memory() for _ in range(2)]
     hy_t = [torch.empty(m, dtype=torch.float64).pin_memory() for _ in range(2)]
     hx, hy = [t.numpy() for t in hx_t], [t.numpy() for t in hy_t]
-    ke = 3 if args.quick else max(10, min(K, 400))
+    # steady-state throughput of the pipelined call: at least 100 calls, so
+    # the pipeline's fill (first upload) and drain (last download) are a
+    # small part of the measured span whatever K is
+    ke = 3 if args.quick else max(100, min(K, 400))
     for i in range(4):
         plan.spmv_host_async(hx[i % 2], hy[i % 2], kernel=kernel)
     stream.synchronize()
@@ -572,12 +608,10 @@ def run_gpu(args, rank, world):
         "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": K, "warmup": args.warmup,
         "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": DATA,
-        "config": {"workload": workload_name(n), "m": m, "n": n, "nnz": nnz, "seed": SEED,
-                   "kernel": "bucketed (auto)" if plan.info["heavy_cols"] else "stream (auto)",
-                   "heavy_band_cols": plan.info["heavy_cols"], "heavy_band_nnz": plan.info["heavy_nnz"],
-                   "tilenum": plan.info["tilenum"], "steps_h_count": plan.info["steps"],
-                   "l2": "inputs larger than L2: matrix streams %.0f MB vs 129 MB L2" % (nnz * 12 / 1e6),
-                   "parallelism": f"replicas x{world}"},
+        "config": bench_config(c, world),
+        "plan": {"kernel": "bucketed (auto)" if plan.info["heavy_cols"] else "stream (auto)",
+                 "heavy_band_cols": plan.info["heavy_cols"], "heavy_band_nnz": plan.info["heavy_nnz"],
+                 "tilenum": plan.info["tilenum"], "steps_h_count": plan.info["steps"]},
         "pct_of_peak": 100.0 * value / world / peak,
         "gflops": 2.0 * nnz * world / (ms_step * 1e-3) / 1e9,
         "rel_err_vs_fp64_oracle": {"normwise": rel[0], "max_over_inf": rel[1]},

@@ -86,12 +86,14 @@ def build_library(force: bool = False, verbose: bool = False) -> str:
     return target
 
 
-def build_oracle(with_reference: bool = True) -> None:
-    """Builds oracle/liboracle.so and, when the reference sources exist on this
-    machine, oracle/_ref/libfastload_ref.so (test infrastructure only)."""
+def build_oracle(reference_src: str | None = None) -> None:
+    """Builds oracle/liboracle.so and, when reference_src names the
+    reference's src/ directory (argument, else the FL_REFERENCE_SRC
+    environment variable; no default), oracle/_ref/libfastload_ref.so from
+    those sources (test infrastructure only)."""
     subprocess.run(["make", "-s", "-C", ORACLE_DIR, "all"], check=True)
-    ref_src = os.environ.get("FL_REFERENCE_SRC", "/root/reference/src")
-    if with_reference and os.path.isdir(ref_src):
+    ref_src = reference_src or os.environ.get("FL_REFERENCE_SRC")
+    if ref_src and os.path.isdir(ref_src):
         subprocess.run(["make", "-s", "-C", ORACLE_DIR, "ref", f"REF_SRC={ref_src}"], check=True)
 
 

@@ -115,6 +115,7 @@ SIGNATURES = [
     ("fl_plan_form_info", C.c_int, [C.c_void_p, C.c_int, C.POINTER(FormInfoC)]),
     ("fl_plan_spmv_form", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
     ("fl_plan_permute_x_k", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("fl_convert_values", C.c_int, [C.c_int, C.c_long, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("fl_batch_create", C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.POINTER(C.c_void_p), C.c_int, C.c_int]),
     ("fl_batch_info", C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_long), C.POINTER(C.c_long),
                                 C.POINTER(C.c_long), C.POINTER(C.c_int)]),

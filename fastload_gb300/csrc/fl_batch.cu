@@ -77,9 +77,7 @@ __global__ void k_batch_vals(const double *src, long n, int vtype, unsigned char
         } else if (vtype == FL_VALUES_F32) {
             ((float *)dst)[i] = (float)v;
         } else {
-            const __nv_bfloat16 hi = __double2bfloat16(v);
-            const __nv_bfloat16 lo = __double2bfloat16(v - (double)__bfloat162float(hi));
-            ((uint32_t *)dst)[i] = (uint32_t)__bfloat16_as_ushort(hi) | ((uint32_t)__bfloat16_as_ushort(lo) << 16);
+            ((uint32_t *)dst)[i] = bf16x2_encode(v);
         }
     }
 }

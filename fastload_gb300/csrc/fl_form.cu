@@ -5,8 +5,9 @@
 // A form is built from the plan's FP64 FastLoad layout: the tile-ordered
 // streams are scattered back into the column-sorted CSC (the inverse of the
 // tile build), the bucketed split is rebuilt with the requested band, and
-// the values are converted to the storage type (round to nearest; a BF16
-// hi+lo pair stores hi = bf16(v) and lo = bf16(v - hi)).
+// the values are converted to the storage type (FP32: round to nearest;
+// BF16 hi+lo: hi = bf16(v) and a 16-bit correction relative to hi, see
+// bf16x2_encode in fl_stream.cuh).
 #include "fl_forms.cuh"
 
 #include <cuda_bf16.h>
@@ -72,12 +73,8 @@ __global__ void k_to_f32(const double *in, float *out, long n) {
 }
 
 __global__ void k_to_bf16x2(const double *in, uint32_t *out, long n) {
-    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-        const double v = in[i];
-        const __nv_bfloat16 hi = __double2bfloat16(v);
-        const __nv_bfloat16 lo = __double2bfloat16(v - (double)__bfloat162float(hi));
-        out[i] = (uint32_t)__bfloat16_as_ushort(hi) | ((uint32_t)__bfloat16_as_ushort(lo) << 16);
-    }
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+        out[i] = bf16x2_encode(in[i]);
 }
 
 static int convert(const DevBuf<double> &src, DevBuf<unsigned char> &dst, int vtype, cudaStream_t s) {
@@ -226,3 +223,18 @@ int permute_x_k(const int *perm, int n, int k, const double *x, void *xs, int to
 }
 
 }  // namespace fl
+
+using namespace fl;
+
+extern "C" int fl_convert_values(int value_type, long n, const double *d_in, void *d_out, void *stream) {
+    clear_error();
+    if (value_type != FL_VALUES_F32 && value_type != FL_VALUES_BF16X2)
+        return fail(FL_ERR_ARG, "convert_values: value type %d (FP32 or BF16 hi+lo)", value_type);
+    if (n < 0 || (n && (!d_in || !d_out))) return fail(FL_ERR_ARG, "convert_values: bad arguments");
+    if (n == 0) return FL_SUCCESS;
+    const cudaStream_t s = (cudaStream_t)stream;
+    if (value_type == FL_VALUES_F32) k_to_f32<<<grid_n(n, 256), 256, 0, s>>>(d_in, (float *)d_out, n);
+    else k_to_bf16x2<<<grid_n(n, 256), 256, 0, s>>>(d_in, (uint32_t *)d_out, n);
+    FL_CUDA(cudaGetLastError());
+    return FL_SUCCESS;
+}

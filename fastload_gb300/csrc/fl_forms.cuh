@@ -2,7 +2,8 @@
 //
 // One template covers every form beside the plain FP64 drop-in kernels:
 //   V  value storage: double (FP64), float (FP32) or bf16x2_t (a BF16 hi+lo
-//      split: v ~ float(hi) + float(lo), hi = bf16(v), lo = bf16(v - hi));
+//      split: hi = bf16(v) and a 16-bit correction relative to hi, 23
+//      significant bits in all; fl_stream.cuh);
 //   K  right-hand sides: x and y row-interleaved (x[col*K + r], y[row*K + r]);
 //   XS x of the heavy band read from shared memory (staged by a TMA bulk copy)
 //      or from global memory (bands wider than shared memory);

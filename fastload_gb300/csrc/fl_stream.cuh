@@ -22,12 +22,38 @@ namespace fl {
 
 constexpr unsigned FULLM = 0xffffffffu;
 
+// BF16 hi+lo value storage, 4 bytes a value.  The high half is hi =
+// bf16(v) (round to nearest even), a plain BF16 that a BF16 consumer can
+// read on its own.  The low half is a signed 16-bit correction d relative to
+// hi: v ~ hi * (1 + d * 2^-22), |d| <= 32767.  Since |v - hi| <= 2^-8 |hi|,
+// d spans the residual with 15 bits, so hi and d together carry 23
+// significant bits: the stored value is within 2^-23 |hi| of v, and the
+// decoded FP32 value (one fma) within (2^-23 + 2^-24) |v|.  (A BF16 low
+// half -- hi + bf16(v - hi) -- keeps 16 significant bits and leaves up to
+// 2^-17 relative error per value, too coarse for a 1e-6 result.)  Values
+// whose hi is zero, infinite, NaN or below 2^-100 in magnitude store d = 0.
 struct bf16x2_t {
     uint32_t u;
 };
 
+constexpr int BF16X2_LO_SHIFT = 22;  // d is the residual in units of 2^-22 |hi|
+
+__device__ __forceinline__ uint32_t bf16x2_encode(double v) {
+    const __nv_bfloat16 h = __double2bfloat16(v);
+    const double hf = (double)__bfloat162float(h);
+    int d = 0;
+    if (fabs(hf) >= 0x1p-100 && fabs(hf) <= 0x1.fep+127) {  // nonzero and finite
+        // v - hf is exact (Sterbenz: hf and v are within a factor of two)
+        const double t = rint((v - hf) / hf * (double)(1 << BF16X2_LO_SHIFT));
+        d = (int)fmin(fmax(t, -32767.0), 32767.0);
+    }
+    return ((uint32_t)__bfloat16_as_ushort(h) << 16) | (uint32_t)(uint16_t)(int16_t)d;
+}
+
 __device__ __forceinline__ float bf16x2_decode(uint32_t u) {
-    return __uint_as_float(u << 16) + __uint_as_float(u & 0xffff0000u);
+    const float hi = __uint_as_float(u & 0xffff0000u);
+    const float d = (float)(int16_t)(u & 0xffffu);
+    return fmaf(hi * 0x1p-22f, d, hi);
 }
 
 __device__ __forceinline__ int ld_stream_i32(const int *p) {

@@ -130,6 +130,21 @@ def _dev(a, dtype):
     return t.contiguous()
 
 
+def convert_values(values, value_type: int = VALUES_F32, stream=None):
+    """FP64 values converted on the device to a form's storage type
+    (fl_convert_values): a float32 tensor for VALUES_F32, an int32 tensor of
+    BF16 hi+lo words (high half bf16(v), low half the 16-bit correction) for
+    VALUES_BF16X2."""
+    torch = _torch()
+    v = _dev(values, torch.float64)
+    if value_type not in (VALUES_F32, VALUES_BF16X2):
+        raise FastLoadArgumentError(f"convert_values: value type {value_type} (VALUES_F32 or VALUES_BF16X2)")
+    out = torch.empty(v.numel(), dtype=torch.float32 if value_type == VALUES_F32 else torch.int32, device=v.device)
+    check(load().fl_convert_values(int(value_type), v.numel(), C.c_void_p(v.data_ptr()), C.c_void_p(out.data_ptr()),
+                                   _stream_handle(stream)))
+    return out
+
+
 class Plan:
     """FastLoad layout of one matrix resident on the current CUDA device."""
 

@@ -348,7 +348,10 @@ int fl_cusparse_spmv_host(int m, int n, int nnz, const int *csr_rowptr,
 /* Value storage of a form. */
 #define FL_VALUES_F64 0    /* FP64 values, FP64 products (x and y FP64) */
 #define FL_VALUES_F32 1    /* FP32 values, FP32 x, FP32 products */
-#define FL_VALUES_BF16X2 2 /* BF16 hi+lo split (v ~ hi + lo), FP32 x, FP32 products */
+#define FL_VALUES_BF16X2 2 /* BF16 hi+lo split, FP32 x, FP32 products: the high
+                              half of each 4-byte value is hi = bf16(v), the low
+                              half a signed 16-bit correction d relative to hi
+                              (v ~ hi (1 + d 2^-22)); 23 significant bits */
 /* Heavy band of a form (columns handled in 32-row slices, one lane per row). */
 #define FL_BAND_AUTO 0     /* automatic: the densest columns (>= 32 nonzeros, up to 128 KB of x: 16,384 FP64 / 32,768 FP32 columns) when they hold >= 1/4 of the matrix; else every column when x gathers have locality, rows are skewed or the matrix has 1M+ nonzeros and 4+ a column; else none */
 #define FL_BAND_NONE (-1)  /* pure FastLoad tile stream (one atomic per run) */
@@ -375,6 +378,13 @@ int fl_plan_spmv_form(fl_plan_t plan, int form_id, int k, const void *d_xs,
 /* xs[i*k + r] = x[perm[i]*k + r], converted to float when to_f32 != 0. */
 int fl_plan_permute_x_k(fl_plan_t plan, int k, int to_f32, const double *d_x,
                         void *d_xs, void *stream);
+
+/* Converts n FP64 values to a form's storage type on the device, exactly as
+ * forms store their values: FL_VALUES_F32 (d_out: n floats, round to
+ * nearest) or FL_VALUES_BF16X2 (d_out: n 32-bit words, high half bf16(v),
+ * low half the 16-bit correction).  Asynchronous on `stream`. */
+int fl_convert_values(int value_type, long n, const double *d_in, void *d_out,
+                      void *stream);
 
 /* ---- batches: many matrices, one persistent launch ---------------------- */
 
@@ -458,8 +468,15 @@ int fl_mlp_destroy(fl_mlp_t mlp);
  *  - n must be at most FL_NOALLOC_MAX_COLS; larger n returns FL_ERR_ARG
  *    with a message (use fl_col_sort or a plan instead).
  *  - The first call on a device looks up the scratch array's device address
- *    (with that device current); make that first call before any stream
- *    capture.
+ *    (with that device current) and keeps it for the life of the process;
+ *    make that first call before any stream capture.  The kept address does
+ *    not survive a reset of the device's context (cudaDeviceReset): do not
+ *    call this entry point on a device after resetting it.
+ *  - With CUDA's lazy module loading, the scratch array (about 3.3 MB) is
+ *    created on a device when this library's module is first loaded there,
+ *    which may be that first call.  An application that reserves the whole
+ *    GPU for its own pool should make the first call on each device (or any
+ *    other call of this library on it) before reserving the pool.
  *  - All calls share the one scratch array, which keeps the last call's
  *    contents (the entry point zeroes what must start at zero).  Calls that
  *    overlap on the GPU -- on different streams or from different host

@@ -22,8 +22,32 @@
 #define FASTLOAD_GB300_COMPAT_H
 
 #include <cstdio>
+#include <cstring>
+#include <iostream>
 
 #include "fastload.h"
+
+/* Under nvcc the replaced src/FastLoad_GPU.h also gave its includers the
+ * CUDA runtime and two error-report macros, which the reference's other
+ * headers (src/CSCSpMV.h) use: the same names here, reporting to stderr
+ * and continuing as the reference does. */
+#if defined(__CUDACC__)
+#include <cuda_runtime.h>
+namespace fastload_compat_detail {
+inline void report_cuda(cudaError_t e, const char *what, const char *file, int line) {
+    if (e != cudaSuccess)
+        std::cerr << "CUDA error at " << file << ":" << line << ": " << cudaGetErrorString(e) << " (" << what
+                  << ")" << std::endl;
+}
+}  // namespace fastload_compat_detail
+#ifndef CHECK_CUDA_ERROR
+#define CHECK_CUDA_ERROR(call) fastload_compat_detail::report_cuda((call), #call, __FILE__, __LINE__)
+#endif
+#ifndef CHECK_LAST_CUDA_ERROR
+#define CHECK_LAST_CUDA_ERROR() \
+    fastload_compat_detail::report_cuda(cudaGetLastError(), "last error", __FILE__, __LINE__)
+#endif
+#endif
 
 /* The reference's format.h defines slide_matrix and the slidesize macro
  * (without an include guard).  When it is already included, use its type;

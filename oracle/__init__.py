@@ -190,3 +190,34 @@ def rel_errors(y, yref):
     ninf = float(np.max(np.abs(yref))) if yref.size else 0.0
     return (float(np.linalg.norm(d)) / n2 if n2 else float(np.linalg.norm(d)),
             float(np.max(np.abs(d))) / ninf if ninf else float(np.max(np.abs(d)) if d.size else 0.0))
+
+
+def bf16x2_split(v):
+    """Numpy restatement of the BF16 hi+lo value storage (no reference
+    counterpart: the storage form is this engine's).  Returns the 32-bit
+    words: high half hi = bf16(v) rounded to nearest even from the FP64
+    value, low half the signed 16-bit correction d = round((v - hi) / hi *
+    2^22) clamped to +-32767 (d = 0 when hi is zero, non-finite or below
+    2^-100 in magnitude)."""
+    v = np.asarray(v, np.float64)
+    with np.errstate(over="ignore", invalid="ignore"):
+        m, e = np.frexp(v)  # v = m 2^e, 0.5 <= |m| < 1
+        # 8 significant bits, round half to even (np.rint); below the normal
+        # range the BF16 spacing is 2^-133
+        hf = np.where(e >= -125, np.ldexp(np.rint(np.ldexp(m, 8)), e - 8), np.rint(np.ldexp(v, 133)) * 2.0 ** -133)
+        hf = np.where(np.isfinite(v), hf, v)
+        hi_b = hf.astype(np.float32).view(np.uint32)  # exact; overflow to +-inf past the BF16 range
+        hf = hi_b.view(np.float32).astype(np.float64)
+        ok = (np.abs(hf) >= 2.0 ** -100) & np.isfinite(hf)
+        d = np.where(ok, np.rint((v - hf) / np.where(ok, hf, 1.0) * 2.0 ** 22), 0.0)
+    d = np.clip(d, -32767, 32767).astype(np.int16)
+    return hi_b | d.view(np.uint16).astype(np.uint32)
+
+
+def bf16x2_value(words):
+    """Decoded FP32 value of BF16 hi+lo words, as the kernels decode it:
+    fma(hi * 2^-22, d, hi), rounded once to FP32."""
+    w = np.asarray(words, np.uint32)
+    hi = (w & np.uint32(0xFFFF0000)).view(np.float32).astype(np.float64)
+    d = (w & np.uint32(0xFFFF)).astype(np.uint16).view(np.int16).astype(np.float64)
+    return (hi * 2.0 ** -22 * d + hi).astype(np.float32)

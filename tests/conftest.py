@@ -16,6 +16,13 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
 
 
+def reference_checkout():
+    """The reference checkout, for the CPU tests that compile its own
+    sources (FL_REFERENCE, else its usual location); None when absent."""
+    path = os.environ.get("FL_REFERENCE", "/root/reference")
+    return path if os.path.isfile(os.path.join(path, "src", "main.cu")) else None
+
+
 def golden_names():
     return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN_DIR, "*.npz")))
 

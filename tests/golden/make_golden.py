@@ -20,7 +20,8 @@ Inputs: the reference's bundled Data/1138_bus.mtx (read with the reference's
 mmio_allinone), the 9x9 matrix of spmv.cu (parsed from that file), seeded
 synthetic matrices and small edge cases.  Run from the repo root:
 
-    make -C oracle all ref && python tests/golden/make_golden.py
+    make -C oracle all ref REF_SRC=<checkout>/src &&
+        FL_REFERENCE=<checkout> python tests/golden/make_golden.py
 """
 from __future__ import annotations
 
@@ -37,7 +38,7 @@ sys.path.insert(0, ROOT)
 from fastload_gb300 import gen  # noqa: E402  (generators only, no CUDA)
 from oracle import ref  # noqa: E402
 
-REF = os.environ.get("FL_REFERENCE", "/root/reference")
+REF = os.environ.get("FL_REFERENCE")  # the reference checkout (its Data/ and spmv.cu); required
 OUT = os.path.dirname(os.path.abspath(__file__))
 
 
@@ -84,6 +85,8 @@ def from_csc(c: gen.CSC):
 
 
 def main():
+    if not REF or not os.path.isdir(REF):
+        sys.exit("make_golden.py: set FL_REFERENCE to the reference checkout (its Data/ and spmv.cu are read)")
     rng = np.random.default_rng(20261203)
     # 1. the reference's bundled matrix, run the way main.cu runs it
     m, n, nnz, sym, rp, ci, v = ref.mmio_read(os.path.join(REF, "Data", "1138_bus.mtx"))

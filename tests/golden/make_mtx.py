@@ -10,7 +10,7 @@ count, duplicates, empty rows, and value spellings whose rounding is hard
 (more than 19 digits, halfway cases, subnormals, the extremes of binary64).
 Run from the repo root:
 
-    make -C oracle all ref && python tests/golden/make_mtx.py
+    make -C oracle all ref REF_SRC=<checkout>/src && python tests/golden/make_mtx.py
 """
 from __future__ import annotations
 

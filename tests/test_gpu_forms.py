@@ -4,9 +4,9 @@ Tolerances (normwise ||y - y*||_2 / ||y*||_2, y* = exactly rounded A x on the
 original FP64 values and x):
   FP64 values               1e-12
   FP32 values, FP32 x       1e-6   (the FP32-path target of the workload)
-  BF16 hi+lo values, FP32 x 2e-5   (hi + lo keeps 16 significant bits, so a
-                                    value carries up to 2^-17 relative error;
-                                    1e-6 is out of its reach -- stated, not hidden)
+  BF16 hi+lo values, FP32 x 1e-6   (hi = bf16(v) plus a 16-bit correction:
+                                    23 significant bits, within 2^-23 + 2^-24
+                                    of each value once decoded)
 Integer-valued matrices (values and x small integers) are exact in every
 form."""
 import numpy as np
@@ -17,7 +17,7 @@ from conftest import golden_names, load_golden
 
 pytestmark = pytest.mark.gpu
 
-TOL = {0: 1e-12, 1: 1e-6, 2: 2e-5}
+TOL = {0: 1e-12, 1: 1e-6, 2: 1e-6}
 INTEGER_CASES = {"bus_i10", "spmv9", "runs", "dups"}
 
 
@@ -122,16 +122,36 @@ def test_full_size_laplacian_forms(gpu, vtype):
         p.check()
 
 
-def test_full_size_zipf_fp32_auto_band(gpu):
+def test_full_size_zipf_auto_band(gpu):
+    """The 2^20-column Zipf(1.8) matrix (27M nonzeros) in FP32 and BF16
+    hi+lo with the automatic heavy band."""
     from fastload_gb300 import gen
 
     c = gen.zipf_columns(1 << 20, 1.8, 50000, seed=2)
     yref = oracle.csc_spmv_dd(c.m, c.n, c.colptr, c.rowidx, c.val, c.x)
     with gpu.Plan.from_csc(c.m, c.n, c.colptr, c.rowidx, c.val) as p:
-        fid = p.add_form(gpu.VALUES_F32, gpu.BAND_AUTO)
-        assert p.form_info(fid)["heavy_cols"] > 0
-        check(run_form(gpu, p, fid, 1, c.x, 1), yref, 1, False, "zipf/f32")
+        for vtype in (gpu.VALUES_F32, gpu.VALUES_BF16X2):
+            fid = p.add_form(vtype, gpu.BAND_AUTO)
+            assert p.form_info(fid)["heavy_cols"] > 0
+            check(run_form(gpu, p, fid, vtype, c.x, 1), yref, vtype, False, f"zipf/v{vtype}")
         p.check()
+
+
+def test_convert_values_matches_oracle(gpu):
+    """The device's storage conversion equals the oracle's restatement bit
+    for bit: BF16 hi+lo words and FP32 values, over many magnitudes, ties,
+    zeros, subnormals and the BF16 overflow threshold."""
+    rng = np.random.default_rng(5)
+    v = rng.standard_normal(200_000) * np.exp(rng.uniform(-80, 80, 200_000))
+    ties = 1.0 + np.arange(1, 256) * 2.0 ** -8  # every tie of the BF16 rounding in [1, 2)
+    special = np.array([0.0, -0.0, 1e-40, -1e-40, 2.0 ** -101, 2.0 ** -99, 3.38e38, 3.4e38, -3.4e38, 1e300,
+                        np.inf, -np.inf])
+    v = np.concatenate([v, ties, -ties, special])
+    w = gpu.convert_values(v, gpu.VALUES_BF16X2).cpu().numpy().view(np.uint32)
+    np.testing.assert_array_equal(w, oracle.bf16x2_split(v))
+    f = gpu.convert_values(v, gpu.VALUES_F32).cpu().numpy()
+    with np.errstate(over="ignore"):
+        np.testing.assert_array_equal(f, v.astype(np.float32))
 
 
 @pytest.mark.parametrize("vtype", [0, 1, 2])

@@ -72,3 +72,32 @@ def test_noalloc_rejects_sizes_beyond_its_scratch(gpu):
     assert rc == -1
     msg = lib.fl_last_error().decode()
     assert "FL_NOALLOC_MAX_COLS" in msg and str(n) in msg
+
+
+def _case(c):
+    deg = np.diff(c.colptr).astype(np.int32)
+    return {"m": c.m, "n": c.n, "nnz": c.nnz, "nnzpercol": deg, "cscptr": c.colptr, "cscrow": c.rowidx,
+            "cscval": c.val, "x": c.x, "perm": np.argsort(deg, kind="stable").astype(np.int32)}
+
+
+def test_noalloc_multi_tile_sizes_twice(gpu):
+    """At the size limit (262,144 columns: 64 radix tiles of 4,096 columns,
+    so the digit histograms and the column-pointer scan span several blocks
+    and the scan recurses), then on about 20,000 columns (5 tiles) with the
+    same shared scratch: both equal fl_col_sort bit for bit, and the
+    permutation is the stable order of the column counts."""
+    from fastload_gb300 import _lib, gen
+
+    lib = _lib.load()
+    cases = (gen.zipf_columns(262144, 1.8, 5000, seed=31), gen.zipf_columns(20011, 1.5, 3000, seed=32))
+    assert cases[0].n == 262144  # FL_NOALLOC_MAX_COLS
+    for c in cases:
+        g = _case(c)
+        t, srow, sval, snnz, sx = gpu.ColSort(g["m"], g["n"], g["nnz"], g["nnzpercol"], g["cscptr"], g["cscrow"],
+                                              g["cscval"], g["x"])
+        got = _noalloc_sort(lib, g)
+        np.testing.assert_array_equal(got["perm"], g["perm"])
+        np.testing.assert_array_equal(got["snnz"], snnz)
+        np.testing.assert_array_equal(got["srow"][:g["nnz"]], srow)
+        np.testing.assert_array_equal(got["sval"][:g["nnz"]], sval)
+        np.testing.assert_array_equal(got["sx"], sx)
