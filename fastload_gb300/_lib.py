@@ -49,6 +49,13 @@ class FormInfoC(C.Structure):
                 ("y_f32", C.c_int), ("device_bytes", C.c_size_t)]
 
 
+class FormOptsC(C.Structure):
+    """fl_form_opts: build and launch options of a form."""
+
+    _fields_ = [("value_type", C.c_int), ("heavy_band", C.c_int), ("y_f32", C.c_int), ("light_item", C.c_int),
+                ("heavy_loop", C.c_int), ("x_stage", C.c_int), ("unit_warps", C.c_int), ("reserved", C.c_int)]
+
+
 class PlanOptsC(C.Structure):
     _fields_ = [("with_reference_arrays", C.c_int), ("heavy_band", C.c_int), ("reserved", C.c_int * 6)]
 
@@ -113,6 +120,9 @@ SIGNATURES = [
     ("fl_plan_load", C.c_int, [C.POINTER(C.c_void_p), C.c_char_p, C.c_void_p]),
     ("fl_plan_add_form", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int)]),
     ("fl_plan_form_info", C.c_int, [C.c_void_p, C.c_int, C.POINTER(FormInfoC)]),
+    ("fl_plan_add_form_opts", C.c_int, [C.c_void_p, C.POINTER(FormOptsC), C.POINTER(C.c_int)]),
+    ("fl_plan_form_opts_get", C.c_int, [C.c_void_p, C.c_int, C.POINTER(FormOptsC)]),
+    ("fl_plan_form_set_launch", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int]),
     ("fl_plan_spmv_form", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
     ("fl_plan_permute_x_k", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("fl_convert_values", C.c_int, [C.c_int, C.c_long, C.c_void_p, C.c_void_p, C.c_void_p]),
@@ -135,6 +145,9 @@ SIGNATURES = [
     ("fl_mlp_grad", C.c_int, [C.c_void_p, c_float_p, c_float_p, c_float_p, C.c_int, c_float_p, c_float_p]),
     ("fl_mlp_train", C.c_int, [C.c_void_p, c_float_p, c_float_p, c_float_p, C.c_int, C.c_int, C.c_float, c_float_p]),
     ("fl_mlp_destroy", C.c_int, [C.c_void_p]),
+    ("fl_tuner_variants", C.c_int, [C.POINTER(FormOptsC), C.c_int]),
+    ("fl_plan_add_tuned_form", C.c_int, [C.c_void_p, C.c_char_p, C.c_int, C.c_int, C.POINTER(C.c_int),
+                                         C.POINTER(C.c_int)]),
     ("fl_col_sort_noalloc", C.c_int, [C.c_int, C.c_int] + [C.c_void_p] * 11),
 ]
 

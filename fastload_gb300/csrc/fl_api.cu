@@ -723,15 +723,43 @@ int fl_plan_spmv_host_async(fl_plan_t p, const double *h_xs, double *h_y, int va
     return FL_SUCCESS;
 }
 
-int fl_plan_add_form(fl_plan_t p, int value_type, int heavy_band, int y_f32, int *form_id) {
+int fl_plan_add_form_opts(fl_plan_t p, const fl_form_opts *opts, int *form_id) {
     clear_error();
-    if (!p || !form_id) return fail(FL_ERR_ARG, "add_form: NULL argument");
+    if (!p || !opts || !form_id) return fail(FL_ERR_ARG, "add_form: NULL argument");
     std::unique_ptr<Form> F(new (std::nothrow) Form());
     if (!F) return fail(FL_ERR_ALLOC, "add_form: host allocation failed");
     FL_CUDA(cudaDeviceSynchronize());
-    FL_TRY(build_form(*F, p->L, value_type, heavy_band, y_f32 != 0, 0));
+    FL_TRY(build_form(*F, p->L, *opts, 0));
     p->forms.push_back(std::move(F));
     *form_id = (int)p->forms.size() - 1;
+    return FL_SUCCESS;
+}
+
+int fl_plan_add_form(fl_plan_t p, int value_type, int heavy_band, int y_f32, int *form_id) {
+    fl_form_opts o = {};
+    o.value_type = value_type;
+    o.heavy_band = heavy_band;
+    o.y_f32 = y_f32 != 0;
+    return fl_plan_add_form_opts(p, &o, form_id);
+}
+
+int fl_plan_form_opts_get(fl_plan_t p, int form_id, fl_form_opts *opts) {
+    clear_error();
+    if (!p || !opts || form_id < 0 || form_id >= (int)p->forms.size())
+        return fail(FL_ERR_ARG, "form_opts_get: bad plan or form id");
+    *opts = p->forms[form_id]->opts;
+    return FL_SUCCESS;
+}
+
+int fl_plan_form_set_launch(fl_plan_t p, int form_id, int heavy_loop, int x_stage) {
+    clear_error();
+    if (!p || form_id < 0 || form_id >= (int)p->forms.size())
+        return fail(FL_ERR_ARG, "form_set_launch: bad plan or form id");
+    fl_form_opts o = p->forms[form_id]->opts;
+    o.heavy_loop = heavy_loop;
+    o.x_stage = x_stage;
+    FL_TRY(check_form_opts(o));
+    p->forms[form_id]->opts = o;
     return FL_SUCCESS;
 }
 

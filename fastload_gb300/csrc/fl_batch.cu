@@ -14,15 +14,6 @@
 #include <cstring>
 #include <vector>
 
-namespace fl {
-
-int run_form_f64(const FormArgs<double, double> &a, int k, bool wide, cudaStream_t s);
-int run_form_f32(const FormArgs<float, double> &a, int k, bool wide, cudaStream_t s);
-int run_form_f32_y32(const FormArgs<float, float> &a, int k, bool wide, cudaStream_t s);
-int run_form_bf16(const FormArgs<bf16x2_t, double> &a, int k, bool wide, cudaStream_t s);
-
-}  // namespace fl
-
 using namespace fl;
 
 struct fl_batch {
@@ -249,6 +240,23 @@ int fl_batch_create(fl_batch_t *out, int count, const fl_plan_t *plans, int valu
         for (int c = b->n_off[i]; c < b->n_off[i + 1]; c++) perm[c] += b->n_off[i];
     }
     sp[b->nslices] = (int)e_off[count];
+    if (vsize(value_type) == 4 && e_off[count] > 0) {
+        // 4-byte values: the stacked band in lane-major packs of four steps
+        // (fl_forms.cuh), values and columns alike
+        const long steps = e_off[count] / 32, ne = p4_entries(steps);
+        DevBuf<unsigned char> pv;
+        DevBuf<int> pc;
+        FL_TRY(pv.alloc((size_t)ne * 4, s));
+        FL_TRY(pc.alloc(ne, s));
+        k_to_p4<uint32_t><<<grid_b(ne, 256), 256, 0, s>>>((const uint32_t *)b->val.get(), steps,
+                                                          (uint32_t *)pv.get(), ne);
+        FL_CUDA(cudaGetLastError());
+        k_to_p4<int><<<grid_b(ne, 256), 256, 0, s>>>(b->col.get(), steps, pc.get(), ne);
+        FL_CUDA(cudaGetLastError());
+        FL_CUDA(cudaStreamSynchronize(s));
+        b->val = std::move(pv);
+        b->col = std::move(pc);
+    }
     // work units over the stacked slices, about four per resident warp
     std::vector<int> ustep, uslice;
     b->split = make_units(sp, e_off[count] / (4L * num_sms() * 32), ustep, uslice);

@@ -69,10 +69,11 @@ __global__ void k_slice_width(const unsigned *rows, const int *rlen, int nslices
 }
 
 // One warp per slice: lane l copies row rows[32s+l]'s band entries to
-// slice_ptr[s] + 32 j + l (zero padding past the row's length).
+// slice_ptr[s] + 32 j + l; past the row's length value 0 and column pad
+// (the band width nh: the zero the shared-memory x staging keeps at x[nh]).
 __global__ void k_slice_fill(const unsigned *rows, const int *rlen, const int *rp, const int *hc,
                              const double *hv, int nrows, int nslices, const int *slice_ptr, double *val,
-                             uint16_t *col, int *col32, int *srow, int *slen) {
+                             uint16_t *col, int *col32, int *srow, int *slen, int pad) {
     const int lane = threadIdx.x & 31;
     long gw = (blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5, nw = ((long)gridDim.x * blockDim.x) >> 5;
     for (long s = gw; s < nslices; s += nw) {
@@ -86,8 +87,8 @@ __global__ void k_slice_fill(const unsigned *rows, const int *rlen, const int *r
         for (int j = 0; j < w; j++) {
             const long dst = base + 32L * j + lane;
             val[dst] = j < len ? hv[src + j] : 0.0;
-            if (col) col[dst] = j < len ? (uint16_t)hc[src + j] : (uint16_t)0;
-            else col32[dst] = j < len ? hc[src + j] : 0;
+            if (col) col[dst] = (uint16_t)(j < len ? hc[src + j] : pad);
+            else col32[dst] = j < len ? hc[src + j] : pad;
         }
     }
 }
@@ -168,9 +169,13 @@ bool make_units(const std::vector<int> &sp, long per_unit, std::vector<int> &uni
 
 int bucket_auto_band(const int *sortnnz, int n, int nnz, cudaStream_t s, int x_bytes) {
     if (n <= 0 || nnz <= 0) return 0;
-    // 16,384 columns of FP64 x, 32,768 of FP32 x: what fits 128 KB of shared
-    // memory beside the per-warp rings
-    const int tail = std::min(n, BK_AUTO_BAND_BYTES / std::max(x_bytes, 1));
+    // FP64: 16,384 columns, 128 KB of x in shared memory beside the per-warp
+    // rings.  4-byte values: 49,152 columns, 192 KB of x (the packed band's
+    // register loop needs no ring, and a wider band leaves fewer nonzeros
+    // to the light part's latency-bound stream: at the 2^20-column Zipf(1.8)
+    // matrix 45.3 against 50.7 us back to back for 32,768 columns)
+    const int budget = x_bytes >= 8 ? BK_AUTO_BAND_BYTES : FM_SMEM_MAX;
+    const int tail = std::min(n, budget / std::max(x_bytes, 1));
     std::vector<int> h(tail);
     FL_TRY(read_ints(s, sortnnz + (n - tail), h.data(), tail));
     int band = 0;
@@ -186,7 +191,7 @@ int bucket_auto_band(const int *sortnnz, int n, int nnz, cudaStream_t s, int x_b
 }
 
 int build_bucket(Bucket &B, int m, int n, int nnz, const int *sortnnz, const int *srow_tmp,
-                 const double *sval_tmp, int nh, cudaStream_t s, bool wide) {
+                 const double *sval_tmp, int nh, cudaStream_t s, bool wide, int unit_warps) {
     nh = std::max(0, std::min(nh, wide ? n : std::min(n, BK_MAX_BAND)));
     if (!wide || nh < n) nh &= ~1;
     const int H0 = n - nh;
@@ -259,13 +264,13 @@ int build_bucket(Bucket &B, int m, int n, int nnz, const int *sortnnz, const int
     }
     FL_TRY(H.row.alloc(32L * H.nslices, s));
     FL_TRY(H.len.alloc(32L * H.nslices, s));
-    // work units: about four per resident warp, so that every warp has work
-    // however the nonzeros fall into slices (short, fat matrices have few
-    // slices of great width, and those are cut)
+    // work units: about four per resident warp (unit_warps), so that every
+    // warp has work however the nonzeros fall into slices (short, fat
+    // matrices have few slices of great width, and those are cut)
     {
         std::vector<int> sp(H.nslices + 1), ustep, uslice;
         FL_TRY(read_ints(s, H.slice_ptr.get(), sp.data(), H.nslices + 1));
-        const long per_unit = (long)sp[H.nslices] / (4L * num_sms() * 32);
+        const long per_unit = (long)sp[H.nslices] / ((unit_warps > 0 ? unit_warps : 4L) * num_sms() * 32);
         H.split = make_units(sp, per_unit, ustep, uslice);
         H.nunits = (int)uslice.size();
         FL_TRY(H.unit_step.alloc(ustep.size(), s));
@@ -278,7 +283,7 @@ int build_bucket(Bucket &B, int m, int n, int nnz, const int *sortnnz, const int
     }
     k_slice_fill<<<grid_cap(32L * H.nslices, 256, 16), 256, 0, s>>>(
         rows.get(), rlen.get(), rp.get(), hc.get(), hv.get(), H.nrows, H.nslices, H.slice_ptr.get(), H.val.get(),
-        narrow ? H.col.get() : nullptr, narrow ? nullptr : H.col32.get(), H.row.get(), H.len.get());
+        narrow ? H.col.get() : nullptr, narrow ? nullptr : H.col32.get(), H.row.get(), H.len.get(), nh);
     FL_CUDA(cudaGetLastError());
     FL_CUDA(cudaStreamSynchronize(s));
     return FL_SUCCESS;
@@ -288,7 +293,6 @@ int build_bucket(Bucket &B, int m, int n, int nnz, const int *sortnnz, const int
 // The FP64 bucketed SpMV is the FP64, one right-hand-side instance of the
 // generic form kernel (fl_forms.cuh): light items through the FastLoad stream,
 // heavy units with x staged in shared memory by a TMA bulk copy.
-int run_form_f64(const FormArgs<double, double> &a, int k, bool wide, cudaStream_t s);
 
 bool bucket_overlap_ok(const Bucket &B) {
     const HeavyBand &H = B.heavy;

@@ -10,7 +10,7 @@
 //
 // File layout (little-endian; offsets in bytes):
 //     0  char     magic[8]      "FLGBPLAN"
-//     8  uint32   version       1
+//     8  uint32   version       2 (1 is read too)
 //    12  uint32   header_bytes  128
 //    16  uint32   byte_order    0x01020304
 //    20  int32    m, n, nnz
@@ -26,7 +26,10 @@
 //        int32    sortnnz[n]    nonzeros per sorted column (ascending)
 //        int32    row[nnz]      tile-ordered row indices
 //        float64  val[nnz]      tile-ordered values
-//        int32    forms[3*nforms]  (value type, heavy band, y_f32) per form
+//        int32    forms[8*nforms]  per form its fl_form_opts: value type,
+//                                  heavy band, y_f32, light item, heavy
+//                                  loop, x staging, units per warp, 0
+//                                  (version 1: the first three only)
 //
 // Hash: 64-bit FNV-1a over little-endian 64-bit words (the tail zero-padded
 // to a full word), then xor-ed with the byte count.  Loading checks the
@@ -48,7 +51,8 @@ namespace fl {
 namespace {
 
 constexpr char kMagic[8] = {'F', 'L', 'G', 'B', 'P', 'L', 'A', 'N'};
-constexpr uint32_t kVersion = 1;
+constexpr uint32_t kVersion = 2;
+constexpr int kFormInts = 8;  // fl_form_opts, as int32 (version 1: 3)
 constexpr uint32_t kHeaderBytes = 128;
 constexpr uint32_t kByteOrder = 0x01020304u;
 constexpr int kMaxForms = 1024;
@@ -155,10 +159,12 @@ extern "C" int fl_plan_save(fl_plan_t p, const char *path) {
     FL_TRY(to_host(row, L.row.get(), L.nnz, s));
     FL_TRY(to_host(val, L.val.get(), L.nnz, s));
     FL_CUDA(cudaStreamSynchronize(s));
+    static_assert(sizeof(fl_form_opts) == kFormInts * sizeof(int32_t), "form options are 8 int32");
     for (const auto &F : p->forms) {
-        forms.push_back(F->vtype);
-        forms.push_back(F->band);
-        forms.push_back(F->yf32);
+        const fl_form_opts &o = F->opts;
+        const int v[kFormInts] = {o.value_type, o.heavy_band, o.y_f32, o.light_item,
+                                  o.heavy_loop, o.x_stage,    o.unit_warps, 0};
+        forms.insert(forms.end(), v, v + kFormInts);
     }
     FileHeader h;
     memset(&h, 0, sizeof h);
@@ -206,22 +212,23 @@ extern "C" int fl_plan_load(fl_plan_t *out, const char *path, void *stream) {
     FileHeader h;
     if (fread(&h, 1, sizeof h, f.f) != sizeof h) return fail(FL_ERR_IO, "plan_load: %s is not a plan file", path);
     if (memcmp(h.magic, kMagic, 8) != 0) return fail(FL_ERR_IO, "plan_load: %s is not a plan file", path);
-    if (h.version != kVersion || h.header_bytes != kHeaderBytes || h.byte_order != kByteOrder)
-        return fail(FL_ERR_IO, "plan_load: %s has version %u / header %u / byte order 0x%08x (expected %u/%u/0x%08x)",
+    if ((h.version != kVersion && h.version != 1) || h.header_bytes != kHeaderBytes || h.byte_order != kByteOrder)
+        return fail(FL_ERR_IO, "plan_load: %s has version %u / header %u / byte order 0x%08x (expected %u or 1/%u/0x%08x)",
                     path, h.version, h.header_bytes, h.byte_order, kVersion, kHeaderBytes, kByteOrder);
+    const int fi = h.version == 1 ? 3 : kFormInts;  // ints per form
     if (hash_bytes(&h, offsetof(FileHeader, header_hash)) != h.header_hash)
         return fail(FL_ERR_IO, "plan_load: %s: header checksum mismatch", path);
     if (h.m < 0 || h.n < 0 || h.nnz < 0 || h.nforms < 0 || h.nforms > kMaxForms || h.heavy < -1 || h.heavy > h.n)
         return fail(FL_ERR_IO, "plan_load: %s: header out of range (m=%d n=%d nnz=%d forms=%d heavy=%d)", path, h.m,
                     h.n, h.nnz, h.nforms, h.heavy);
     const int m = h.m, n = h.n, nnz = h.nnz;
-    const long expect = (long)kHeaderBytes + 8L * n + 12L * nnz + 12L * h.nforms;
+    const long expect = (long)kHeaderBytes + 8L * n + 12L * nnz + 4L * fi * h.nforms;
     if (fseek(f.f, 0, SEEK_END) != 0) return fail(FL_ERR_IO, "plan_load: cannot seek in %s", path);
     const long size = ftell(f.f);
     if (size != expect)
         return fail(FL_ERR_IO, "plan_load: %s has %ld bytes, the header implies %ld", path, size, expect);
     if (fseek(f.f, kHeaderBytes, SEEK_SET) != 0) return fail(FL_ERR_IO, "plan_load: cannot seek in %s", path);
-    std::vector<int> perm(n), sortnnz(n), row(nnz), forms(3 * (size_t)h.nforms);
+    std::vector<int> perm(n), sortnnz(n), row(nnz), forms((size_t)fi * h.nforms);
     std::vector<double> val(nnz);
     FL_TRY(read_all(f.f, perm.data(), perm.size() * 4, path));
     FL_TRY(read_all(f.f, sortnnz.data(), sortnnz.size() * 4, path));
@@ -287,7 +294,19 @@ extern "C" int fl_plan_load(fl_plan_t *out, const char *path, void *stream) {
     for (int i = 0; i < h.nforms; i++) {
         std::unique_ptr<Form> F(new (std::nothrow) Form());
         if (!F) return fail(FL_ERR_ALLOC, "plan_load: host allocation failed");
-        FL_TRY(build_form(*F, L, forms[3 * i], forms[3 * i + 1], forms[3 * i + 2] != 0, s));
+        fl_form_opts o = {};
+        const int *v = forms.data() + (size_t)fi * i;
+        o.value_type = v[0];
+        o.heavy_band = v[1];
+        o.y_f32 = v[2] != 0;
+        if (fi == kFormInts) {
+            o.light_item = v[3];
+            o.heavy_loop = v[4];
+            o.x_stage = v[5];
+            o.unit_warps = v[6];
+            o.reserved = v[7];
+        }
+        FL_TRY(build_form(*F, L, o, s));
         p->forms.push_back(std::move(F));
     }
     cudaError_t e = cudaStreamSynchronize(s);

@@ -14,11 +14,6 @@
 
 namespace fl {
 
-int run_form_f64(const FormArgs<double, double> &a, int k, bool wide, cudaStream_t s);
-int run_form_f32(const FormArgs<float, double> &a, int k, bool wide, cudaStream_t s);
-int run_form_f32_y32(const FormArgs<float, float> &a, int k, bool wide, cudaStream_t s);
-int run_form_bf16(const FormArgs<bf16x2_t, double> &a, int k, bool wide, cudaStream_t s);
-
 static int grid_n(long n, int threads, int per_sm = 8) {
     long b = (n + threads - 1) / threads;
     long cap = (long)num_sms() * per_sm;
@@ -87,13 +82,54 @@ static int convert(const DevBuf<double> &src, DevBuf<unsigned char> &dst, int vt
     return FL_SUCCESS;
 }
 
-int build_form(Form &F, const Layout &L, int vtype, int band, int yf32, cudaStream_t s) {
-    if (vtype != FL_VALUES_F64 && vtype != FL_VALUES_F32 && vtype != FL_VALUES_BF16X2)
-        return fail(FL_ERR_ARG, "add_form: unknown value type %d", vtype);
-    if (yf32 && vtype != FL_VALUES_F32) return fail(FL_ERR_ARG, "add_form: FP32 y needs FP32 values");
+// Values (converted, 4 bytes each) and columns of a slice-layout band to
+// the packed layout of 4-byte bands; the band's column arrays are replaced.
+int pack_band_p4(HeavyBand &H, const DevBuf<unsigned char> &vals, DevBuf<unsigned char> &out, cudaStream_t s) {
+    const long steps = H.padded / 32, ne = p4_entries(steps);
+    FL_TRY(out.alloc((size_t)ne * 4, s));
+    k_to_p4<uint32_t><<<grid_n(ne, 256), 256, 0, s>>>((const uint32_t *)vals.get(), steps, (uint32_t *)out.get(), ne);
+    FL_CUDA(cudaGetLastError());
+    if (H.col.get()) {
+        DevBuf<uint16_t> c;
+        FL_TRY(c.alloc(ne, s));
+        k_to_p4<uint16_t><<<grid_n(ne, 256), 256, 0, s>>>(H.col.get(), steps, c.get(), ne);
+        FL_CUDA(cudaGetLastError());
+        FL_CUDA(cudaStreamSynchronize(s));
+        H.col = std::move(c);
+    } else {
+        DevBuf<int> c;
+        FL_TRY(c.alloc(ne, s));
+        k_to_p4<int><<<grid_n(ne, 256), 256, 0, s>>>(H.col32.get(), steps, c.get(), ne);
+        FL_CUDA(cudaGetLastError());
+        FL_CUDA(cudaStreamSynchronize(s));
+        H.col32 = std::move(c);
+    }
+    return FL_SUCCESS;
+}
+
+int check_form_opts(const fl_form_opts &o) {
+    if (o.value_type != FL_VALUES_F64 && o.value_type != FL_VALUES_F32 && o.value_type != FL_VALUES_BF16X2)
+        return fail(FL_ERR_ARG, "add_form: unknown value type %d", o.value_type);
+    if (o.y_f32 && o.value_type != FL_VALUES_F32) return fail(FL_ERR_ARG, "add_form: FP32 y needs FP32 values");
+    if (o.heavy_band < FL_BAND_ALL) return fail(FL_ERR_ARG, "add_form: heavy band %d", o.heavy_band);
+    if (o.light_item != 0 && (o.light_item < 128 || o.light_item > 8192 || o.light_item % 128))
+        return fail(FL_ERR_ARG, "add_form: light item %d (0, or 128..8192 in steps of 128)", o.light_item);
+    if (o.heavy_loop < FL_HEAVY_AUTO || o.heavy_loop > FL_HEAVY_REGS)
+        return fail(FL_ERR_ARG, "add_form: heavy loop %d", o.heavy_loop);
+    if (o.x_stage < FL_XSTAGE_AUTO || o.x_stage > FL_XSTAGE_GLOBAL)
+        return fail(FL_ERR_ARG, "add_form: x staging %d", o.x_stage);
+    if (o.unit_warps < 0 || o.unit_warps > 64) return fail(FL_ERR_ARG, "add_form: unit_warps %d (0..64)", o.unit_warps);
+    if (o.reserved != 0) return fail(FL_ERR_ARG, "add_form: reserved field must be 0");
+    return FL_SUCCESS;
+}
+
+int build_form(Form &F, const Layout &L, const fl_form_opts &o, cudaStream_t s) {
+    FL_TRY(check_form_opts(o));
+    const int vtype = o.value_type, band = o.heavy_band;
     F.vtype = vtype;
-    F.yf32 = yf32;
+    F.yf32 = o.y_f32 != 0;
     F.band = band;
+    F.opts = o;
     const int m = L.m, n = L.n, nnz = L.nnz;
     // the column-sorted CSC, recovered from the tile streams
     DevBuf<int> srow;
@@ -115,14 +151,27 @@ int build_form(Form &F, const Layout &L, int vtype, int band, int yf32, cudaStre
     } else {
         return fail(FL_ERR_ARG, "add_form: heavy band %d", band);
     }
-    FL_TRY(build_bucket(F.B, m, n, nnz, L.sortnnz.get(), srow.get(), sval.get(), nh, s, wide));
+    FL_TRY(build_bucket(F.B, m, n, nnz, L.sortnnz.get(), srow.get(), sval.get(), nh, s, wide, o.unit_warps));
     F.wide = F.B.heavy.nh > 65535;
+    // light items: as asked, else for 4-byte values at most 1,024 nonzeros
+    // (the light stream's items are serial chains on one warp; beside the
+    // faster packed band, shorter chains end with it: 45.3 against 47.8 us
+    // at the 2^20-column Zipf(1.8) matrix)
+    const int auto_item = item_nnz_for(nnz);
+    const int item = o.light_item > 0 ? o.light_item : (vtype == FL_VALUES_F64 ? auto_item : std::min(auto_item, 1024));
+    if (F.B.light.nnz > 0 && item != auto_item) FL_TRY(build_regions_sized(F.B.light, item, F.B.light.regions, s));
     if (vtype != FL_VALUES_F64) {
         FL_TRY(convert(F.B.light.val, F.lval, vtype, s));
-        FL_TRY(convert(F.B.heavy.val, F.hval, vtype, s));
+        HeavyBand &H = F.B.heavy;
+        if (H.nnz > 0 && H.nh > 0) {
+            // the band in lane-major packs of four steps (fl_forms.cuh)
+            DevBuf<unsigned char> conv;
+            FL_TRY(convert(H.val, conv, vtype, s));
+            FL_TRY(pack_band_p4(H, conv, F.hval, s));
+        }
         FL_CUDA(cudaStreamSynchronize(s));
         F.B.light.val.release();
-        F.B.heavy.val.release();
+        H.val.release();
     }
     FL_CUDA(cudaStreamSynchronize(s));
     return FL_SUCCESS;
@@ -158,6 +207,8 @@ static FormArgs<V, Y> form_args(Form &F, const V *lval, const V *hval, const voi
     a.err_host = nullptr;
     a.heavy_mode = 0;
     a.bulk = 0;
+    a.heavy_loop = F.opts.heavy_loop;
+    a.x_stage = F.opts.x_stage;
     return a;
 }
 

@@ -67,6 +67,9 @@ struct FormArgs {
     // host-mapped status word of a synchronous host call (nullptr: none):
     // an expired wait is also reported there, so the call needs no readback
     int *err_host;
+    // launch options of the form (host side: they pick the instantiation)
+    int heavy_loop = FL_HEAVY_AUTO;
+    int x_stage = FL_XSTAGE_AUTO;
 };
 
 // An expired bounded wait: bits into the launch's status word (and the host
@@ -391,6 +394,257 @@ __device__ __forceinline__ void heavy_unit_ring(const FormArgs<V, Y> &a, int sl,
     __syncwarp();
 }
 
+// ---- heavy band of 4-byte values: lane-major packs of four steps ---------
+// FP32 and BF16 hi+lo bands keep their entries in packs of four steps with
+// each lane's four entries adjacent: entry (global step S, lane l) at
+//     128 * (S / 4) + 4 * l + S % 4.
+// A lane reads its four values of a pack with one 16-byte load and its four
+// columns with one 8-byte (16-bit columns) or 16-byte (32-bit) load, and a
+// warp's loads of one pack are contiguous.  Against one entry per load this
+// cuts the instructions a nonzero costs by about four, which is what bounds
+// a 4-byte band (its bytes per nonzero are half of FP64's).  Entries a row
+// does not have (a lane past its row's length inside a slice) hold value 0
+// and column nh, and the shared-memory staging of x keeps a zero at x[nh],
+// so the ring loop needs no length test.
+constexpr int P4_STAGES = 2;                // packs in a lane's ring (a power of two)
+constexpr int P4_VB = 32 * 4 * 4;           // value bytes of a pack (512)
+constexpr int P4_CB = 32 * 4 * 2;           // 16-bit column bytes of a pack (256)
+constexpr int P4_SB = P4_VB + P4_CB;        // ring stage
+constexpr int P4_RING_WARP = P4_STAGES * P4_SB;
+
+__host__ __device__ __forceinline__ long p4_index(long S, int l) { return 128 * (S >> 2) + 4 * l + (S & 3); }
+// Entries of a packed band array of `steps` steps: whole packs, plus one
+// pack of padding (the loops read whole packs).
+inline long p4_entries(long steps) { return ((steps + 3) / 4 + 1) * 128; }
+
+// Slice-layout array (entry j of step S, lane l at 32 S + l; `steps` steps)
+// to packed layout; entries past the last step are zero.
+template <typename T>
+__global__ void k_to_p4(const T *__restrict__ in, long steps, T *__restrict__ out, long nout) {
+    for (long d = blockIdx.x * (long)blockDim.x + threadIdx.x; d < nout; d += (long)gridDim.x * blockDim.x) {
+        const long S = 4 * (d >> 7) + (d & 3);
+        const int l = (int)((d >> 2) & 31);
+        out[d] = S < steps ? in[32 * S + l] : (T)0;
+    }
+}
+
+__device__ __forceinline__ void cp_async8(void *smem_dst, const void *gsrc) {
+    const uint32_t d = (uint32_t)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(d), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ uint4 ld_stream_v4(const void *p) {
+    uint4 r;
+    asm("ld.global.nc.L1::no_allocate.v4.u32 {%0, %1, %2, %3}, [%4];"
+        : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w)
+        : "l"(p));
+    return r;
+}
+__device__ __forceinline__ uint2 ld_stream_v2(const void *p) {
+    uint2 r;
+    asm("ld.global.nc.L1::no_allocate.v2.u32 {%0, %1}, [%2];" : "=r"(r.x), "=r"(r.y) : "l"(p));
+    return r;
+}
+
+// A unit's walk over its slices in global steps: the current slice's first
+// and end step, this lane's row and length in it, the first step of the
+// unit's part of it, and the next slice's values, fetched one slice ahead.
+struct SliceWalk {
+    int s0, bnd, len, r, jb, sl;
+    int nbnd, nlen, nr;
+};
+
+template <typename V, typename Y>
+__device__ __forceinline__ void walk_fetch_next(SliceWalk &w, const FormArgs<V, Y> &a, int T1, int lane) {
+    if (w.bnd < T1) {
+        w.nbnd = __ldg(a.slice_ptr + w.sl + 2) >> 5;
+        w.nlen = __ldg(a.hlen + 32 * (w.sl + 1) + lane);
+        w.nr = __ldg(a.hrow + 32 * (w.sl + 1) + lane);
+    }
+}
+
+template <typename V, typename Y>
+__device__ __forceinline__ void walk_init(SliceWalk &w, const FormArgs<V, Y> &a, int sl, int T0, int T1, int lane) {
+    w.sl = sl;
+    w.s0 = __ldg(a.slice_ptr + sl) >> 5;
+    w.bnd = __ldg(a.slice_ptr + sl + 1) >> 5;
+    w.len = __ldg(a.hlen + 32 * sl + lane);
+    w.r = __ldg(a.hrow + 32 * sl + lane);
+    w.jb = T0 - w.s0;
+    w.nbnd = w.nlen = w.nr = 0;
+    walk_fetch_next(w, a, T1, lane);
+}
+
+// Step S, the last of a part (S + 1 ends the slice or the unit), is done:
+// the part's sums go to y (when this lane's row has entries in the part)
+// and the walk moves to the next slice when the slice ended.
+template <typename V, int K, typename Y>
+__device__ __forceinline__ void walk_end(SliceWalk &w, const FormArgs<V, Y> &a, float acc[K], int S, int T1,
+                                         int lane) {
+    if (w.len > w.jb) heavy_flush<float, K, Y>(a.heavy_mode, a.y, w.r, acc);
+#pragma unroll
+    for (int q = 0; q < K; q++) acc[q] = 0.f;
+    if (S + 1 == w.bnd) {
+        w.sl++;
+        w.s0 = w.bnd;
+        w.jb = 0;
+        w.len = w.nlen;
+        w.r = w.nr;
+        w.bnd = w.nbnd;
+        walk_fetch_next(w, a, T1, lane);
+    }
+}
+
+// Heavy unit [T0, T1) of a packed 4-byte band through a per-lane ring in
+// shared memory (K = 1, x and 16-bit columns staged): each lane copies its
+// own 16 bytes of values and 8 bytes of columns of each pack with cp.async
+// into its own slots, P4_STAGES packs deep, so no warp barrier is needed;
+// cp.async.wait_group (a hardware wait) says when a pack is in.
+template <typename V, typename Y>
+__device__ __forceinline__ void heavy_unit_ring_p4(const FormArgs<V, Y> &a, int sl, int T0, int T1,
+                                                   const float *xsrc, unsigned char *ring, int lane) {
+    static_assert(sizeof(V) == 4, "packed bands hold 4-byte values");
+    if (T0 >= T1) return;
+    const int P0 = T0 >> 2, np = ((T1 + 3) >> 2) - P0;
+    const char *vsrc = (const char *)(a.hval + 128L * P0) + 16 * lane;
+    const char *csrc = (const char *)(a.hcol16 + 128L * P0) + 8 * lane;
+    unsigned char *lv = ring + 16 * lane, *lc = ring + P4_VB + 8 * lane;
+    auto issue = [&](int k) {
+        if (k < np) {
+            const int o = (k & (P4_STAGES - 1)) * P4_SB;
+            cp_async16(lv + o, vsrc);
+            cp_async8(lc + o, csrc);
+            vsrc += P4_VB;
+            csrc += P4_CB;
+        }
+        cp_async_commit();
+    };
+#pragma unroll
+    for (int k = 0; k < P4_STAGES; k++) issue(k);
+    SliceWalk w;
+    walk_init(w, a, sl, T0, T1, lane);
+    float acc[1] = {0.f};
+    int S0 = P0 * 4;
+    for (int k = 0; k < np; k++, S0 += 4) {
+        cp_async_wait<P4_STAGES - 1>();
+        const int o = (k & (P4_STAGES - 1)) * P4_SB;
+        const uint4 v = *(const uint4 *)(lv + o);
+        const uint2 c = *(const uint2 *)(lc + o);
+        const float x0 = xsrc[c.x & 0xffffu], x1 = xsrc[c.x >> 16], x2 = xsrc[c.y & 0xffffu], x3 = xsrc[c.y >> 16];
+        if (S0 >= T0 && S0 + 4 < w.bnd && S0 + 4 < T1) {
+            // the pack lies inside the unit and inside one slice, not at its end
+            acc[0] = fmaf(VT<V>::from_bits(v.x), x0, acc[0]);
+            acc[0] = fmaf(VT<V>::from_bits(v.y), x1, acc[0]);
+            acc[0] = fmaf(VT<V>::from_bits(v.z), x2, acc[0]);
+            acc[0] = fmaf(VT<V>::from_bits(v.w), x3, acc[0]);
+        } else {
+            const uint32_t vv[4] = {v.x, v.y, v.z, v.w};
+            const float xx[4] = {x0, x1, x2, x3};
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const int S = S0 + q;
+                if (S >= T0 && S < T1) {
+                    acc[0] = fmaf(VT<V>::from_bits(vv[q]), xx[q], acc[0]);
+                    if (S + 1 == w.bnd || S + 1 == T1) walk_end<V, 1, Y>(w, a, acc, S, T1, lane);
+                }
+            }
+        }
+        issue(k + P4_STAGES);
+    }
+    cp_async_wait<0>();
+}
+
+// Heavy unit [T0, T1) of a packed 4-byte band with loads held in registers:
+// x in shared memory too wide for the ring beside it, x read through the
+// cache, or K right-hand sides.  Groups of PG packs, the next group's loads
+// issued before the current group is computed; entries past a row's length
+// are skipped (x read from global memory has no zero slot).
+template <typename V, int K, bool XS, bool C16, typename Y>
+__device__ __forceinline__ void heavy_unit_p4(const FormArgs<V, Y> &a, int sl, int T0, int T1, const float *xsrc,
+                                              int lane) {
+    static_assert(sizeof(V) == 4, "packed bands hold 4-byte values");
+    constexpr int PG = K == 1 ? 2 : 1;
+    if (T0 >= T1) return;
+    const int P0 = T0 >> 2, np = ((T1 + 3) >> 2) - P0;
+    auto load = [&](int k, uint4 vv[PG], uint4 cc[PG]) {
+#pragma unroll
+        for (int g = 0; g < PG; g++) {
+            if (k + g < np) {
+                const long e = 128L * (P0 + k + g) + 4 * lane;
+                vv[g] = ld_stream_v4(a.hval + e);
+                if constexpr (C16) {
+                    const uint2 t = ld_stream_v2(a.hcol16 + e);  // unpacked where used: two registers held
+                    cc[g] = make_uint4(t.x, t.y, 0u, 0u);
+                } else {
+                    cc[g] = ld_stream_v4(a.hcol32 + e);
+                }
+            }
+        }
+    };
+    SliceWalk w;
+    walk_init(w, a, sl, T0, T1, lane);
+    float acc[K];
+#pragma unroll
+    for (int q = 0; q < K; q++) acc[q] = 0.f;
+    uint4 v[PG], c[PG];
+    load(0, v, c);
+    for (int k = 0; k < np; k += PG) {
+        uint4 nv[PG], nc[PG];
+        load(k + PG, nv, nc);
+#pragma unroll
+        for (int g = 0; g < PG; g++) {
+            if (k + g < np) {
+                const int S0 = 4 * (P0 + k + g);
+                const uint32_t vv[4] = {v[g].x, v[g].y, v[g].z, v[g].w};
+                uint32_t cc[4];
+                if constexpr (C16) {
+                    cc[0] = c[g].x & 0xffffu;
+                    cc[1] = c[g].x >> 16;
+                    cc[2] = c[g].y & 0xffffu;
+                    cc[3] = c[g].y >> 16;
+                } else {
+                    cc[0] = c[g].x;
+                    cc[1] = c[g].y;
+                    cc[2] = c[g].z;
+                    cc[3] = c[g].w;
+                }
+                if (S0 >= T0 && S0 + 4 < w.bnd && S0 + 4 < T1) {
+                    const int j0 = S0 - w.s0;
+#pragma unroll
+                    for (int q = 0; q < 4; q++) {
+                        if (j0 + q < w.len) {
+                            float xv[K];
+                            load_xk<float, K, XS>(xsrc + (size_t)cc[q] * K, xv);
+                            const float f = VT<V>::from_bits(vv[q]);
+#pragma unroll
+                            for (int r = 0; r < K; r++) acc[r] = fmaf(f, xv[r], acc[r]);
+                        }
+                    }
+                } else {
+#pragma unroll
+                    for (int q = 0; q < 4; q++) {
+                        const int S = S0 + q;
+                        if (S >= T0 && S < T1) {
+                            if (S - w.s0 < w.len) {
+                                float xv[K];
+                                load_xk<float, K, XS>(xsrc + (size_t)cc[q] * K, xv);
+                                const float f = VT<V>::from_bits(vv[q]);
+#pragma unroll
+                                for (int r = 0; r < K; r++) acc[r] = fmaf(f, xv[r], acc[r]);
+                            }
+                            if (S + 1 == w.bnd || S + 1 == T1) walk_end<V, K, Y>(w, a, acc, S, T1, lane);
+                        }
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int g = 0; g < PG; g++) {
+            v[g] = nv[g];
+            c[g] = nc[g];
+        }
+    }
+}
+
 // Whether the light columns' x is in (acquire: its bytes are visible to
 // the reading thread afterwards).
 template <typename V, typename Y>
@@ -433,6 +687,8 @@ __global__ void __launch_bounds__(FM_THREADS, 1) k_spmv_form(const FormArgs<V, Y
     const bool use_band = a.nh > 0 && a.nslices > 0;
     if (XS && use_band) {
         const uint32_t bytes = (uint32_t)a.nh * K * (uint32_t)sizeof(X);
+        // x[nh] = 0 (16 bytes): the column of a packed band's padding entries
+        if (tid < 4) ((uint32_t *)(fm_smem + bytes))[tid] = 0u;
         if (a.bulk) {
             if (tid == 0) {
                 asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
@@ -490,8 +746,14 @@ __global__ void __launch_bounds__(FM_THREADS, 1) k_spmv_form(const FormArgs<V, Y
             staged = true;
         }
         const int sl = __ldg(a.unit_slice + ui), T0 = __ldg(a.unit_step + ui), T1 = __ldg(a.unit_step + ui + 1);
-        if constexpr (RING) {
-            const size_t xb = ((size_t)a.nh * K * sizeof(X) + 127) & ~(size_t)127;
+        // the rings start past x and its 16 bytes of zeros (x[nh])
+        const size_t xb = ((size_t)a.nh * K * sizeof(X) + 16 + 127) & ~(size_t)127;
+        if constexpr (sizeof(V) == 4) {
+            if constexpr (RING)
+                heavy_unit_ring_p4<V, Y>(a, sl, T0, T1, xsrc, fm_smem + xb + (size_t)(tid >> 5) * P4_RING_WARP, lane);
+            else
+                heavy_unit_p4<V, K, XS, C16, Y>(a, sl, T0, T1, xsrc, lane);
+        } else if constexpr (RING) {
             heavy_unit_ring<V, Y>(a, sl, T0, T1, xsrc, fm_smem + xb + (size_t)(tid >> 5) * ring_warp_bytes<V>(), lane);
         } else {
             heavy_unit<V, K, XS, C16, Y>(a, sl, T0, T1, xsrc, lane);
@@ -657,14 +919,15 @@ template <typename V, typename Y>
 int dispatch_form(const FormArgs<V, Y> &a, int k, bool wide_cols, cudaStream_t s) {
     using X = typename VT<V>::X;
     const size_t smem = (size_t)a.nh * k * sizeof(X);
-    const bool xs_smem = a.nh > 0 && !wide_cols && smem <= (size_t)FM_SMEM_MAX;
-    const size_t dyn = xs_smem ? smem : 0;
+    const bool xs_smem = a.x_stage != FL_XSTAGE_GLOBAL && a.nh > 0 && !wide_cols && smem <= (size_t)FM_SMEM_MAX;
+    const size_t dyn = xs_smem ? smem + 16 : 0;  // x and 16 bytes of zeros (x[nh])
     if (k == 1) {
         // the heavy band through per-warp shared-memory rings when x and the
         // rings fit beside each other
-        const size_t xb = (smem + 127) & ~(size_t)127;
-        const size_t ring = (size_t)(FM_THREADS / 32) * ring_warp_bytes<V>();
-        const bool use_ring = xs_smem && a.nslices > 0 && xb + ring <= (size_t)SMEM_OPTIN;
+        const size_t xb = (smem + 16 + 127) & ~(size_t)127;
+        const size_t ring = (size_t)(FM_THREADS / 32) * (sizeof(V) == 4 ? (size_t)P4_RING_WARP : ring_warp_bytes<V>());
+        const bool use_ring =
+            a.heavy_loop != FL_HEAVY_REGS && xs_smem && a.nslices > 0 && xb + ring <= (size_t)SMEM_OPTIN;
         if (a.x_ready) {
             // x still arriving (FP64 host call): only the staged-band kernels
             if constexpr (std::is_same<V, double>::value && std::is_same<Y, double>::value) {
@@ -685,5 +948,12 @@ int dispatch_form(const FormArgs<V, Y> &a, int k, bool wide_cols, cudaStream_t s
     }
     return fail(FL_ERR_ARG, "spmv_form: k=%d (supported: 1, 8)", k);
 }
+
+// One instantiation set per value / y type, in its own translation unit
+// (fl_form_f64.cu, fl_form_f32.cu, fl_form_bf16.cu).
+int run_form_f64(const FormArgs<double, double> &a, int k, bool wide, cudaStream_t s);
+int run_form_f32(const FormArgs<float, double> &a, int k, bool wide, cudaStream_t s);
+int run_form_f32_y32(const FormArgs<float, float> &a, int k, bool wide, cudaStream_t s);
+int run_form_bf16(const FormArgs<bf16x2_t, double> &a, int k, bool wide, cudaStream_t s);
 
 }  // namespace fl

@@ -189,6 +189,7 @@ struct Form {
     int vtype = 0;             // FL_VALUES_F64 / F32 / BF16X2
     int yf32 = 0;              // y accumulated in FP32 instead of FP64
     int band = 0;              // heavy band requested (FL_BAND_*)
+    fl_form_opts opts = {};    // the options it was built with (launch options current)
     bool wide = false;         // band columns stored as 32-bit indices
     Bucket B;
     DevBuf<unsigned char> lval, hval;  // converted values (F32 / BF16X2 forms)
@@ -271,8 +272,9 @@ int zero_device(void *p, size_t bytes, cudaStream_t s);
 // Bucketed form: build from the column-sorted CSC (device) and run.
 // wide: allow a band of up to all n columns (x then read from global memory
 // by the form kernels); otherwise the band is capped at bucket_max_band().
+// unit_warps: heavy work units per resident warp (0: 4).
 int build_bucket(Bucket &B, int m, int n, int nnz, const int *sortnnz, const int *srow_tmp,
-                 const double *sval_tmp, int nh, cudaStream_t s, bool wide = false);
+                 const double *sval_tmp, int nh, cudaStream_t s, bool wide = false, int unit_warps = 0);
 // The light columns' x (xs[0, H0)) still arriving while the bucket kernel
 // runs (the overlapped host call): it is in once *flag reaches epoch;
 // err_host is the device view of a host-mapped word that receives the
@@ -310,7 +312,9 @@ int num_sms();
 int untile_layout(const Layout &L, DevBuf<int> &srow, DevBuf<double> &sval, cudaStream_t s);
 
 // Forms (fl_form.cu): build from a plan's FP64 layout, run.
-int build_form(Form &F, const Layout &L, int vtype, int band, int yf32, cudaStream_t s);
+int build_form(Form &F, const Layout &L, const fl_form_opts &o, cudaStream_t s);
+// Range checks of form options (FL_ERR_ARG with a message).
+int check_form_opts(const fl_form_opts &o);
 int spmv_form(Form &F, int k, const void *xs, void *y, int accumulate, cudaStream_t s);
 int permute_x_k(const int *perm, int n, int k, const double *x, void *xs, int to_f32, cudaStream_t s);
 

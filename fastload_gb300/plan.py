@@ -11,7 +11,7 @@ import struct
 
 import numpy as np
 
-from ._lib import FastLoadArgumentError, FormInfoC, PlanInfoC, PlanOptsC, SlideMatrixC, check, load
+from ._lib import FastLoadArgumentError, FormInfoC, FormOptsC, PlanInfoC, PlanOptsC, SlideMatrixC, check, load
 from .host import SlideMatrix
 
 KERNEL_AUTO = 0
@@ -24,6 +24,8 @@ INPUT_CSC = 1
 VALUES_F64 = 0
 VALUES_F32 = 1
 VALUES_BF16X2 = 2
+HEAVY_AUTO, HEAVY_RING, HEAVY_REGS = 0, 1, 2   # FL_HEAVY_*
+XSTAGE_AUTO, XSTAGE_GLOBAL = 0, 1            # FL_XSTAGE_*
 BAND_AUTO = 0
 BAND_NONE = -1
 BAND_ALL = -2
@@ -65,11 +67,12 @@ def plan_file_sections(path) -> dict:
     """The arrays of a plan file (numpy views of its bytes)."""
     h = plan_file_header(path)
     n, nnz, nf = h["n"], h["nnz"], h["nforms"]
+    fi = 3 if h["version"] == 1 else 8  # ints per form: fl_form_opts (version 1: value type, band, y_f32)
     with open(path, "rb") as f:
         f.seek(_HEADER.size)
         out = {"perm": np.fromfile(f, "<i4", n), "sortnnz": np.fromfile(f, "<i4", n),
                "row": np.fromfile(f, "<i4", nnz), "val": np.fromfile(f, "<f8", nnz),
-               "forms": np.fromfile(f, "<i4", 3 * nf).reshape(nf, 3)}
+               "forms": np.fromfile(f, "<i4", fi * nf).reshape(nf, fi)}
     return out
 
 
@@ -286,13 +289,28 @@ class Plan:
         return y
 
     # -- forms ---------------------------------------------------------------
-    def add_form(self, value_type: int = VALUES_F32, heavy_band: int = BAND_AUTO, y_f32: bool = False) -> int:
+    def add_form(self, value_type: int = VALUES_F32, heavy_band: int = BAND_AUTO, y_f32: bool = False,
+                 light_item: int = 0, heavy_loop: int = HEAVY_AUTO, x_stage: int = XSTAGE_AUTO,
+                 unit_warps: int = 0) -> int:
         """Adds a storage form (FP64 / FP32 / BF16 hi+lo values) with the given
-        heavy band; returns its id for spmv_form."""
+        heavy band and build / launch options (fl_form_opts; 0 = automatic);
+        returns its id for spmv_form."""
+        o = FormOptsC(int(value_type), int(heavy_band), int(y_f32), int(light_item), int(heavy_loop), int(x_stage),
+                      int(unit_warps), 0)
         fid = C.c_int(-1)
-        check(load().fl_plan_add_form(self._h, int(value_type), int(heavy_band), int(y_f32), C.byref(fid)))
+        check(load().fl_plan_add_form_opts(self._h, C.byref(o), C.byref(fid)))
         self._form_kinds[fid.value] = (int(value_type), bool(y_f32))
         return fid.value
+
+    def form_opts(self, form_id: int) -> dict:
+        """The options a form was built with (fl_plan_form_opts_get)."""
+        o = FormOptsC()
+        check(load().fl_plan_form_opts_get(self._h, int(form_id), C.byref(o)))
+        return {k: getattr(o, k) for k, _ in FormOptsC._fields_}
+
+    def set_form_launch(self, form_id: int, heavy_loop: int = HEAVY_AUTO, x_stage: int = XSTAGE_AUTO) -> None:
+        """Changes a form's launch options (heavy loop, x staging) in place."""
+        check(load().fl_plan_form_set_launch(self._h, int(form_id), int(heavy_loop), int(x_stage)))
 
     def _kinds(self, form_id: int) -> tuple[int, bool]:
         """(value type, y is FP32) of a form, from the library on first use

@@ -369,6 +369,44 @@ typedef struct fl_form_info {
 int fl_plan_add_form(fl_plan_t plan, int value_type, int heavy_band, int y_f32,
                      int *form_id);
 int fl_plan_form_info(fl_plan_t plan, int form_id, fl_form_info *info);
+
+/* Heavy-band loop of a form (fl_form_opts.heavy_loop). */
+#define FL_HEAVY_AUTO 0  /* the ring where it applies, else loads held in registers */
+#define FL_HEAVY_RING 1  /* band values and columns streamed through shared-memory
+                            rings by cp.async (needs the band's x in shared memory
+                            and room for the rings beside it; else as REGS) */
+#define FL_HEAVY_REGS 2  /* band loads held in registers, a group ahead */
+/* Where the heavy band reads x (fl_form_opts.x_stage). */
+#define FL_XSTAGE_AUTO 0   /* staged in shared memory (TMA bulk copy) when it fits */
+#define FL_XSTAGE_GLOBAL 1 /* read through the cache, never staged */
+
+/* Build and launch options of a form.  Fields after y_f32 at 0 take the
+ * automatic choice; fl_plan_add_form is fl_plan_add_form_opts with them 0. */
+typedef struct fl_form_opts {
+    int value_type; /* FL_VALUES_* */
+    int heavy_band; /* FL_BAND_* or a column count */
+    int y_f32;      /* y accumulated in FP32 (FP32 values only) */
+    int light_item; /* nonzeros per work item of the light columns' FastLoad
+                       stream: 0 automatic (about two items per warp of the
+                       GPU, 128..2048), else 128..8192 in steps of 128 */
+    int heavy_loop; /* FL_HEAVY_* */
+    int x_stage;    /* FL_XSTAGE_* */
+    int unit_warps; /* heavy-band work units per resident warp: 0 automatic
+                       (4), else 1..64 */
+    int reserved;   /* must be 0 */
+} fl_form_opts;
+
+/* Adds a form built with the given options (FL_ERR_ARG for values out of
+ * range); *form_id receives its index. */
+int fl_plan_add_form_opts(fl_plan_t plan, const fl_form_opts *opts,
+                          int *form_id);
+/* The options a form was built with (automatic choices left at 0). */
+int fl_plan_form_opts_get(fl_plan_t plan, int form_id, fl_form_opts *opts);
+/* Changes the launch options of a built form (heavy loop, x staging);
+ * nothing is rebuilt.  Not to be called while the form's SpMVs may be
+ * enqueued from another thread. */
+int fl_plan_form_set_launch(fl_plan_t plan, int form_id, int heavy_loop,
+                            int x_stage);
 /* y = A xs (or += when accumulate) for k right-hand sides (k = 1 or 8):
  * xs[(sorted column)*k + r] (double for FP64 forms, float otherwise; see
  * fl_plan_permute_x_k), y[row*k + r] (double, or float for y_f32 forms).
@@ -447,6 +485,33 @@ int fl_mlp_grad(fl_mlp_t mlp, const float *X, const float *T, const float *M,
 int fl_mlp_train(fl_mlp_t mlp, const float *X, const float *T, const float *M,
                  int B, int epochs, float lr, float *losses);
 int fl_mlp_destroy(fl_mlp_t mlp);
+
+/* ---- tuned forms --------------------------------------------------------- */
+
+/* value_type of a tuner variant that takes the caller's value type. */
+#define FL_TUNE_REQUESTED (-1)
+
+/* The tuner's variant table: the form options the autotuner times and the
+ * network chooses among, in the order of the network's outputs.  Copies up
+ * to `max` entries into out (may be NULL) and returns the table's length.
+ * value_type is FL_TUNE_REQUESTED (the caller's value type) or
+ * FL_VALUES_BF16X2 (BF16 hi+lo storage, offered to callers asking for FP32
+ * values: both meet the same 1e-6 error bar). */
+int fl_tuner_variants(fl_form_opts *out, int max);
+
+/* Adds the form the learned tuner predicts fastest for this plan's matrix:
+ * the plan's 24 features (fl_plan_features) go through the network stored
+ * in model_path (written by the tuner's training, its variant table equal
+ * to fl_tuner_variants) on the GPU, and the variant with the lowest
+ * predicted time among those allowed is built.  Allowed: for value_type
+ * FL_VALUES_F64 the FP64 variants; for FL_VALUES_F32 the FP32 and the BF16
+ * hi+lo variants (FP32 only when y_f32).  *form_id receives the form,
+ * *variant (may be NULL) the chosen row of the variant table.  FL_ERR_IO
+ * for a missing or malformed model file, FL_ERR_ARG for a model trained on
+ * another variant table.  Synchronises the device. */
+int fl_plan_add_tuned_form(fl_plan_t plan, const char *model_path,
+                           int value_type, int y_f32, int *form_id,
+                           int *variant);
 
 /* ---- allocation-free column sort -------------------------------------- */
 

@@ -173,3 +173,38 @@ def test_heavy_band_paths_agree(gpu, vtype):
             assert info["heavy_cols"] == (c.n if band == gpu.BAND_ALL else band)
             check(run_form(gpu, p, fid, vtype, c.x, 1), yref, vtype, False, f"v{vtype}/band{band}")
         p.check()
+
+
+@pytest.mark.parametrize("vtype", [0, 1, 2])
+def test_form_options_match_oracle(gpu, vtype):
+    """Every build / launch option of a form (light item size, heavy loop,
+    x staging, units per warp; fl_form_opts) computes the same product
+    within the form's tolerance, including the shared-memory ring with a
+    unit boundary inside a pack and the register loop with x read through
+    the cache.  Launch options changed in place take effect."""
+    from fastload_gb300 import gen
+
+    c = gen.zipf_columns(70000, 1.6, 5000, seed=23)
+    yref = oracle.csc_spmv_dd(c.m, c.n, c.colptr, c.rowidx, c.val, c.x)
+    with gpu.Plan.from_csc(c.m, c.n, c.colptr, c.rowidx, c.val) as p:
+        for band in (gpu.BAND_AUTO, 4096, gpu.BAND_ALL):
+            for light in (0, 128, 1024):
+                for heavy, xst in ((1, 0), (2, 0), (2, 1)):
+                    for units in (0, 1, 16):
+                        fid = p.add_form(vtype, band, light_item=light, heavy_loop=heavy, x_stage=xst,
+                                         unit_warps=units)
+                        o = p.form_opts(fid)
+                        assert (o["light_item"], o["heavy_loop"], o["x_stage"], o["unit_warps"]) == \
+                            (light, heavy, xst, units)
+                        check(run_form(gpu, p, fid, vtype, c.x, 1), yref, vtype, False,
+                              f"v{vtype}/b{band}/l{light}/h{heavy}/x{xst}/u{units}")
+        fid = p.add_form(vtype, 4096)
+        for heavy, xst in ((1, 0), (2, 0), (2, 1), (0, 0)):
+            p.set_form_launch(fid, heavy, xst)
+            assert (p.form_opts(fid)["heavy_loop"], p.form_opts(fid)["x_stage"]) == (heavy, xst)
+            check(run_form(gpu, p, fid, vtype, c.x, 1), yref, vtype, False, f"launch h{heavy}/x{xst}")
+        for bad in (dict(light_item=100), dict(light_item=9000), dict(heavy_loop=3), dict(x_stage=2),
+                    dict(unit_warps=65)):
+            with pytest.raises(gpu.FastLoadError):
+                p.add_form(vtype, gpu.BAND_AUTO, **bad)
+        p.check()

@@ -85,15 +85,19 @@ def test_forms_survive_round_trip(gpu, tmp_path):
 
     c = gen.zipf_columns(30000, 1.8, 4000, seed=9)
     x = np.random.default_rng(2).uniform(-1, 1, c.n * 8)
-    specs = [(gpu.VALUES_F32, gpu.BAND_ALL, False), (gpu.VALUES_BF16X2, gpu.BAND_AUTO, False),
-             (gpu.VALUES_F32, gpu.BAND_NONE, True), (gpu.VALUES_F64, 256, False)]
+    specs = [(gpu.VALUES_F32, gpu.BAND_ALL, False, {}), (gpu.VALUES_BF16X2, gpu.BAND_AUTO, False, {}),
+             (gpu.VALUES_F32, gpu.BAND_NONE, True, {}), (gpu.VALUES_F64, 256, False, {}),
+             (gpu.VALUES_F32, 2048, False, dict(light_item=512, heavy_loop=2, x_stage=1, unit_warps=8))]
     f = tmp_path / "forms.flplan"
     with gpu.Plan.from_csc(c.m, c.n, c.colptr, c.rowidx, c.val) as a:
-        ids = [a.add_form(v, band, y_f32=y32) for v, band, y32 in specs]
+        ids = [a.add_form(v, band, y_f32=y32, **o) for v, band, y32, o in specs]
         a.save(f)
         with gpu.Plan.load(f) as b:
-            for fid, (v, band, y32) in zip(ids, specs):
+            for fid, (v, band, y32, o) in zip(ids, specs):
                 assert a.form_info(fid) == b.form_info(fid)
+                assert a.form_opts(fid) == b.form_opts(fid)
+                for k, val in o.items():
+                    assert b.form_opts(fid)[k] == val
                 for k in (1, 8):
                     xs_a = a.permute_x_k(torch.from_numpy(x[:c.n * k]).cuda(), k=k, to_f32=v != 0)
                     xs_b = b.permute_x_k(torch.from_numpy(x[:c.n * k]).cuda(), k=k, to_f32=v != 0)
@@ -183,7 +187,7 @@ def test_invalid_content_with_valid_checksums(gpu, tmp_path):
     variant("unsorted_counts", ERR_ARG, sortnnz=unsorted)
     variant("tilenum", ERR_IO, tilenum=hdr["tilenum"] + 1)
     variant("heavy_range", ERR_IO, heavy=c.n + 1)
-    sec["forms"] = np.array([[7, 0, 0]], np.int32)
+    sec["forms"] = np.array([[7, 0, 0, 0, 0, 0, 0, 0]], np.int32)
     variant("form_type", ERR_ARG, nforms=1)
     # the valid file still loads after all of that
     with gpu.Plan.load(f) as b:
