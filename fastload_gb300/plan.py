@@ -7,6 +7,7 @@ PyTorch tensors provide the device memory and the current stream.
 from __future__ import annotations
 
 import ctypes as C
+import os
 import struct
 
 import numpy as np
@@ -322,13 +323,17 @@ class Plan:
         return k
 
     def add_tuned_form(self, value_type: int = VALUES_F32, y_f32: bool = False, model=None) -> tuple[int, str]:
-        """Adds a form whose heavy band the learned tuner picks for this
-        matrix (tuner.choose: the plan's features through the trained MLP on
-        the GPU).  Returns (form id, chosen variant)."""
+        """Adds the form the learned tuner predicts fastest for this matrix,
+        through the C ABI (fl_plan_add_tuned_form: the plan's features through
+        the trained network on the GPU; FP32 callers may get BF16 hi+lo
+        storage).  Returns (form id, chosen variant's name)."""
         from . import tuner
 
-        variant, band = tuner.choose(self, value_type, model)
-        return self.add_form(value_type, band, y_f32=y_f32), variant
+        path = os.fspath(model or tuner.MODEL)
+        fid, var = C.c_int(-1), C.c_int(-1)
+        check(load().fl_plan_add_tuned_form(self._h, path.encode(), int(value_type), int(y_f32), C.byref(fid),
+                                            C.byref(var)))
+        return fid.value, tuner.VARIANTS[var.value]
 
     def form_info(self, form_id: int) -> dict:
         i = FormInfoC()

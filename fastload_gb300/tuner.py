@@ -1,43 +1,98 @@
-"""Learned tuner: picks the heavy band (bucket threshold) / kernel variant of a
-matrix from 24 features with a small MLP trained on the project's own
-exhaustive autotuner timings.
+"""Learned tuner: picks a matrix's complete form configuration from 24
+plan features with a small MLP trained on the project's own exhaustive
+autotuner timings.
 
-Variants (one class each):
-    none   FastLoad tile stream only (no heavy band; one atomic per run)
-    2048   densest 2048 sorted columns as row slices, x in shared memory
-    8192   densest 8192 columns
-    max    the widest band whose x fits shared memory (24576 FP64 / 49152 FP32)
-    all    every column as row slices (rows owned by one lane, no atomics)
-    auto   the library's static rule (plan default) -- the method without the tuner
+The search space is the library's variant table (fl_tuner_variants, one
+network output each), for the caller's value type and, for callers asking
+for FP32 values, the BF16 hi+lo storage (both meet the 1e-6 error bar):
+
+    default   the library's automatic choices (the method without the tuner)
+    none      the FastLoad tile stream alone, light items auto / 512 / 1024
+    all       every column as row slices (rows owned by one lane), heavy
+              units 4 or 2 per warp
+    band      the 8,192 / 24,576 / 49,152 densest columns as row slices
+              x light items auto / 512 / 1024
+              x heavy loop: shared-memory ring, registers with x staged in
+                shared memory, registers with x read through the cache
 
 The training set: seeded matrices of five families (uniform rows, Zipf
 column degrees, banded, block-diagonal, row-skewed) generated on the GPU
 (fl_gen_fill), n log-uniform in [1e4, 4e6], nnz log-uniform in [1e5, 6e7],
-FP64 or FP32 values.  The network (24 -> 64 -> 64 -> 6, ReLU) regresses
-log2(t_variant / t_best) and is trained on the GPU by the library's own
-forward/backward/Adam kernels (fl_mlp_*); the autotuner's measurements are
-what regret is measured against.
+FP64 or FP32 values.  Every variant the matrix's caller may use is built
+and timed (calls back to back: the steady state of repeated SpMVs).  The
+network (24 -> 64 -> 64 -> one output per variant, ReLU) regresses
+log2(t_variant / t_best), the variants a matrix may not use masked out, and
+is trained on the GPU by the library's own forward/backward/Adam kernels
+(fl_mlp_*); the autotuner's measurements are what regret is measured
+against.  The trained network is stored in the library's model format, which
+fl_plan_add_tuned_form reads, so C callers get the tuned form through the C
+ABI.
 
     python -m fastload_gb300.tuner collect --count 2200 --out data.npz
+    python -m fastload_gb300.tuner train --data data.npz
     python -m fastload_gb300.tuner evaluate --data data.npz
 """
 from __future__ import annotations
 
 import argparse
-import os
 import ctypes as C
 import json
+import os
 import time
 
 import numpy as np
 
-from ._lib import FastLoadArgumentError, check, load
+from ._lib import FastLoadArgumentError, FormOptsC, check, load
 
 FAMILIES = ("uniform", "zipf", "banded", "blockdiag", "rowskew")
-VARIANTS = ("none", "2048", "8192", "max", "all", "auto")
 N_FEATURES = 24
 N_RANGE = (1e4, 4e6)
 NNZ_RANGE = (1e5, 6e7)
+TUNE_REQUESTED = -1  # FL_TUNE_REQUESTED: the caller's value type
+_OPT_FIELDS = tuple(k for k, _ in FormOptsC._fields_)
+
+
+def variant_table() -> list[dict]:
+    """The library's variant table (fl_tuner_variants), as option dicts."""
+    n = load().fl_tuner_variants(None, 0)
+    arr = (FormOptsC * n)()
+    load().fl_tuner_variants(arr, n)
+    return [{k: int(getattr(o, k)) for k in _OPT_FIELDS} for o in arr]
+
+
+def variant_name(o: dict) -> str:
+    parts = ["req" if o["value_type"] == TUNE_REQUESTED else "bf16x2",
+             "band=" + {0: "auto", -1: "none", -2: "all"}.get(o["heavy_band"], str(o["heavy_band"]))]
+    if o["light_item"]:
+        parts.append(f"light={o['light_item']}")
+    if o["heavy_loop"]:
+        parts.append({1: "ring", 2: "regs"}[o["heavy_loop"]])
+    if o["x_stage"]:
+        parts.append("xglobal")
+    if o["unit_warps"]:
+        parts.append(f"units={o['unit_warps']}")
+    return "|".join(parts)
+
+
+TABLE = variant_table()
+VARIANTS = tuple(variant_name(o) for o in TABLE)
+DEFAULT = VARIANTS.index("req|band=auto")   # the library's automatic choices
+PLAIN = VARIANTS.index("req|band=none")     # the FastLoad tile stream alone
+
+
+def allowed(value_type: int) -> np.ndarray:
+    """Variants a caller asking for value_type (0 FP64, 1 FP32) may get: its
+    own type, plus BF16 hi+lo storage for FP32 callers."""
+    return np.array([o["value_type"] == TUNE_REQUESTED or (o["value_type"] == 2 and value_type == 1)
+                     for o in TABLE])
+
+
+def resolved(o: dict, value_type: int) -> dict:
+    """A variant's options for a caller of value_type."""
+    r = dict(o)
+    if r["value_type"] == TUNE_REQUESTED:
+        r["value_type"] = int(value_type)
+    return r
 
 
 # ------------------------------------------------------------ generation --
@@ -115,38 +170,49 @@ def features(plan, value_type: int) -> np.ndarray:
 
 
 # ------------------------------------------------------------- autotune --
-def variant_band(variant: str, value_type: int) -> int:
-    from .plan import BAND_ALL, BAND_AUTO, BAND_NONE
-
-    return {"none": BAND_NONE, "2048": 2048, "8192": 8192, "max": 24576 if value_type == 0 else 49152,
-            "all": BAND_ALL, "auto": BAND_AUTO}[variant]
-
-
-def autotune(plan, x, value_type: int, reps: int = 5) -> np.ndarray:
-    """Exhaustive: builds every variant as a form of the plan and times one
-    SpMV (median of reps, L2 flushed before each).  Returns ms per variant."""
+def _time_calls(fn, reps: int) -> float:
+    """Mean device ms of fn() over reps calls back to back (after two
+    untimed); a device sleep ahead of the start event lets the host enqueue
+    the calls first, so small matrices are not timed at the host's pace."""
     import torch
 
-    flush = torch.empty(64 << 20, dtype=torch.float32, device="cuda")
-    xs = plan.permute_x_k(x, k=1, to_f32=value_type != 0)
-    y = torch.empty(plan.m, dtype=torch.float64, device="cuda")
+    fn()
+    fn()
     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    times = np.zeros(len(VARIANTS))
-    for vi, v in enumerate(VARIANTS):
-        band = variant_band(v, value_type)
-        if isinstance(band, int) and band > plan.n:
-            band = -2  # wider than the matrix: every column
-        fid = plan.add_form(value_type, band)
-        plan.spmv_form(fid, xs, y)
-        ts = []
-        for _ in range(reps):
-            flush.zero_()
-            a.record()
-            plan.spmv_form(fid, xs, y)
-            b.record()
-            b.synchronize()
-            ts.append(a.elapsed_time(b))
-        times[vi] = float(np.median(ts))
+    torch.cuda._sleep(600_000)
+    a.record()
+    for _ in range(reps):
+        fn()
+    b.record()
+    b.synchronize()
+    return a.elapsed_time(b) / reps
+
+
+def autotune(plan, x, value_type: int, reps: int = 8) -> np.ndarray:
+    """Exhaustive over the variant table: every variant value_type's caller
+    may use is built as a form of the plan (variants that differ only in
+    launch options share one build) and timed.  Returns ms per variant, NaN
+    where the variant is not allowed."""
+    import torch
+
+    times = np.full(len(TABLE), np.nan)
+    ok = allowed(value_type)
+    xs = {}
+    y = torch.empty(plan.m, dtype=torch.float64, device="cuda")
+    groups: dict = {}
+    for i, o in enumerate(TABLE):
+        if ok[i]:
+            r = resolved(o, value_type)
+            key = (r["value_type"], r["heavy_band"], r["light_item"], r["unit_warps"])
+            groups.setdefault(key, []).append((i, r["heavy_loop"], r["x_stage"]))
+    for (vt, band, light, units), members in groups.items():
+        fid = plan.add_form(vt, band, light_item=light, unit_warps=units)
+        f32 = vt != 0
+        if f32 not in xs:
+            xs[f32] = plan.permute_x_k(x, k=1, to_f32=f32)
+        for i, heavy, xst in members:
+            plan.set_form_launch(fid, heavy, xst)
+            times[i] = _time_calls(lambda: plan.spmv_form(fid, xs[f32], y), reps)
     plan.check()
     return times
 
@@ -155,8 +221,10 @@ def collect(count: int, seed: int = 5, out: str | None = None, log_every: int = 
     rng = np.random.default_rng(seed)
     X, T, meta = [], [], []
     t0 = time.time()
+
     def pack():
-        return {"X": np.array(X, np.float32).reshape(-1, N_FEATURES), "T": np.array(T, np.float64),
+        return {"X": np.array(X, np.float32).reshape(-1, N_FEATURES),
+                "T": np.array(T, np.float64).reshape(-1, len(TABLE)),
                 "meta": np.array([json.dumps(m) for m in meta]), "variants": np.array(VARIANTS)}
 
     for i in range(count):
@@ -184,7 +252,7 @@ def collect(count: int, seed: int = 5, out: str | None = None, log_every: int = 
 class Network:
     """24 -> 64 -> 64 -> K MLP on the GPU (fl_mlp_*), with feature scaling."""
 
-    def __init__(self, n_in=N_FEATURES, h1=64, h2=64, n_out=len(VARIANTS), seed=1):
+    def __init__(self, n_in=N_FEATURES, h1=64, h2=64, n_out=len(TABLE), seed=1):
         h = C.c_void_p()
         check(load().fl_mlp_create(C.byref(h), n_in, h1, h2, n_out, C.c_ulonglong(seed)))
         self._h = h
@@ -239,20 +307,28 @@ class Network:
         return float(loss[0]), g
 
     def fit(self, X, times, epochs=3000, lr=3e-3) -> np.ndarray:
-        """Trains on features X and measured times (ms per variant)."""
+        """Trains on features X and measured times (ms per variant, NaN for
+        variants the matrix may not use, which the loss masks out)."""
         X = self._mat(X, self.shape[0], "fit X")
-        Tg = self._mat(targets(times), self.shape[3], "fit times", X.shape[0])
+        tg, mask = targets(times), mask_of(times)
+        Tg = self._mat(tg, self.shape[3], "fit times", X.shape[0])
+        M = self._mat(mask, self.shape[3], "fit mask", X.shape[0])
         self.mu = X.mean(0)
         self.sd = X.std(0) + 1e-6
         Xn = np.ascontiguousarray((X - self.mu) / self.sd, np.float32)
         losses = np.empty(epochs, np.float32)
-        check(load().fl_mlp_train(self._h, self._fp(Xn), self._fp(Tg), None, Xn.shape[0], epochs, C.c_float(lr),
-                                  losses.ctypes.data_as(C.POINTER(C.c_float))))
+        check(load().fl_mlp_train(self._h, self._fp(Xn), self._fp(Tg), self._fp(M), Xn.shape[0], epochs,
+                                  C.c_float(lr), losses.ctypes.data_as(C.POINTER(C.c_float))))
         return losses
 
-    def predict(self, X) -> np.ndarray:
+    def predict(self, X, allow=None) -> np.ndarray:
+        """Variant with the lowest predicted time per row of X, among the
+        allowed ones (allow: boolean rows or one row; None = all)."""
         Xn = (np.asarray(X, np.float32) - self.mu) / self.sd
-        return np.argmin(self.forward_raw(Xn), axis=1)
+        out = self.forward_raw(Xn).astype(np.float64)
+        if allow is not None:
+            out = np.where(np.broadcast_to(np.asarray(allow, bool), out.shape), out, np.inf)
+        return np.argmin(out, axis=1)
 
     def close(self):
         if self._h:
@@ -266,64 +342,86 @@ class Network:
             pass
 
 
-MODEL = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tuner_data", "model.npz")
+MODEL = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tuner_data", "model.fltuner")
+_MAGIC = b"FLTUNER1"
 
 
 def save_model(net: Network, path: str) -> None:
-    """Weights, feature scaling, shape and variant names of a trained network."""
-    np.savez_compressed(path, params=net.params(), mu=net.mu, sd=net.sd, shape=np.array(net.shape),
-                        variants=np.array(VARIANTS))
+    """The trained network in the library's model format (fl_tune.cu):
+    magic, shape, feature scaling, parameters, the variant table."""
+    n_in, h1, h2, n_out = net.shape
+    opts = np.array([[o[k] for k in _OPT_FIELDS] for o in TABLE], "<i4")
+    with open(path, "wb") as f:
+        f.write(_MAGIC)
+        f.write(np.array([n_in, h1, h2, n_out, len(TABLE), 0, 0, 0], "<i4").tobytes())
+        f.write(np.asarray(net.mu, "<f4").tobytes())
+        f.write(np.asarray(net.sd, "<f4").tobytes())
+        f.write(net.params().astype("<f4").tobytes())
+        f.write(opts.tobytes())
 
 
 def load_model(path: str = MODEL) -> Network:
     """The trained network of `path` on the current device."""
-    with np.load(path) as z:
-        shape = tuple(int(v) for v in z["shape"])
-        if tuple(str(v) for v in z["variants"]) != VARIANTS:
-            raise ValueError(f"{path}: variants {list(z['variants'])} differ from {list(VARIANTS)}")
-        net = Network(*shape)
-        net.set_params(z["params"])
-        net.mu = z["mu"].astype(np.float32)
-        net.sd = z["sd"].astype(np.float32)
+    raw = open(path, "rb").read()
+    if raw[:8] != _MAGIC:
+        raise ValueError(f"{path}: not a tuner model")
+    n_in, h1, h2, n_out, nv = (int(v) for v in np.frombuffer(raw, "<i4", 5, 8))
+    if nv != len(TABLE) or n_out != nv:
+        raise ValueError(f"{path}: {nv} variants, the library has {len(TABLE)}")
+    net = Network(n_in, h1, h2, n_out)
+    o = 40
+    net.mu = np.frombuffer(raw, "<f4", n_in, o).copy()
+    net.sd = np.frombuffer(raw, "<f4", n_in, o + 4 * n_in).copy()
+    o += 8 * n_in
+    net.set_params(np.frombuffer(raw, "<f4", net.num_params, o))
+    o += 4 * net.num_params
+    opts = np.frombuffer(raw, "<i4", 8 * nv, o).reshape(nv, 8)
+    if any(dict(zip(_OPT_FIELDS, (int(v) for v in row))) != t for row, t in zip(opts, TABLE)):
+        raise ValueError(f"{path}: variant table differs from the library's")
     return net
 
 
 _LOADED: dict = {}
 
 
-def choose(plan, value_type: int, model: str | None = None) -> tuple[str, int]:
-    """(variant, heavy band) the trained network predicts fastest for this
-    plan's matrix in the given value type."""
+def choose(plan, value_type: int, model: str | None = None) -> tuple[int, str]:
+    """(variant index, name) the trained network predicts fastest for this
+    plan's matrix among the variants a value_type caller may use -- the
+    choice fl_plan_add_tuned_form makes through the C ABI."""
     path = model or MODEL
     net = _LOADED.get(path)
     if net is None:
         net = _LOADED[path] = load_model(path)
-    v = VARIANTS[int(net.predict(features(plan, value_type)[None, :])[0])]
-    band = variant_band(v, value_type)
-    if band > plan.n:
-        band = variant_band("all", value_type)
-    return v, band
+    i = int(net.predict(features(plan, value_type)[None, :], allowed(value_type))[0])
+    return i, VARIANTS[i]
+
+
+def mask_of(times) -> np.ndarray:
+    return np.isfinite(np.asarray(times, np.float64)).astype(np.float32)
 
 
 def targets(times) -> np.ndarray:
-    """log2(t_variant / t_best) per matrix: 0 for the best variant."""
+    """log2(t_variant / t_best) per matrix over the timed variants: 0 for the
+    best, 0 (masked) where a variant was not timed."""
     t = np.asarray(times, np.float64)
-    return np.log2(t / t.min(axis=1, keepdims=True)).astype(np.float32)
+    best = np.nanmin(t, axis=1, keepdims=True)
+    return np.nan_to_num(np.log2(t / best), nan=0.0).astype(np.float32)
 
 
 def evaluate(pred: np.ndarray, times: np.ndarray) -> dict:
     """Regret of predicted variants against the exhaustive best, and speedup
-    over the method without the tuner (the 'auto' rule) and over the plain
-    tile stream ('none')."""
+    over the method without the tuner (the library default) and over the
+    plain tile stream."""
     t = np.asarray(times, np.float64)
     idx = np.arange(len(t))
     chosen = t[idx, pred]
-    best = t.min(axis=1)
+    best = np.nanmin(t, axis=1)
     regret = chosen / best - 1.0
-    auto = t[:, VARIANTS.index("auto")]
-    none = t[:, VARIANTS.index("none")]
+    auto = t[:, DEFAULT]
+    none = t[:, PLAIN]
     return {
         "matrices": int(len(t)),
+        "variants": int(t.shape[1]),
         "mean_regret": float(regret.mean()),
         "median_regret": float(np.median(regret)),
         "frac_within_10pct": float((regret <= 0.10).mean()),
@@ -335,13 +433,18 @@ def evaluate(pred: np.ndarray, times: np.ndarray) -> dict:
     }
 
 
-def train_and_evaluate(data: dict, n_train: int = 2000, epochs: int = 3000, seed: int = 1) -> dict:
+def train_and_evaluate(data: dict, n_train: int = 2000, epochs: int = 3000, seed: int = 1, save: str | None = None):
     X, T = np.asarray(data["X"]), np.asarray(data["T"])
     net = Network(seed=seed)
     losses = net.fit(X[:n_train], T[:n_train], epochs=epochs)
-    res = {"train": evaluate(net.predict(X[:n_train]), T[:n_train]),
-           "heldout": evaluate(net.predict(X[n_train:]), T[n_train:]) if len(X) > n_train else None,
+    allow = np.isfinite(T)
+    res = {"train": evaluate(net.predict(X[:n_train], allow[:n_train]), T[:n_train]),
+           "heldout": (evaluate(net.predict(X[n_train:], allow[n_train:]), T[n_train:])
+                       if len(X) > n_train else None),
            "final_loss": float(losses[-1]) if len(losses) else None, "epochs": epochs}
+    if save:
+        save_model(net, save)
+        res["model"] = save
     net.close()
     return res
 
@@ -370,15 +473,7 @@ def main():
     with np.load(a.data) as z:
         data = {k: z[k] for k in z.files}
     if a.cmd == "train":
-        X, T = np.asarray(data["X"]), np.asarray(data["T"])
-        net = Network(seed=a.seed)
-        losses = net.fit(X[:a.train], T[:a.train], epochs=a.epochs)
-        save_model(net, a.out)
-        res = {"train": evaluate(net.predict(X[:a.train]), T[:a.train]),
-               "heldout": evaluate(net.predict(X[a.train:]), T[a.train:]) if len(X) > a.train else None,
-               "final_loss": float(losses[-1]), "model": a.out}
-        net.close()
-        print(json.dumps(res))
+        print(json.dumps(train_and_evaluate(data, a.train, a.epochs, a.seed, save=a.out)))
     else:
         print(json.dumps(train_and_evaluate(data, a.train, a.epochs)))
 

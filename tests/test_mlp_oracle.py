@@ -28,14 +28,38 @@ def test_numpy_mlp_gradient_matches_finite_differences():
 
 
 def test_tuner_targets_and_regret():
+    """Targets are log2(t / t_best) over the timed variants; untimed (NaN)
+    variants are masked out; regret is against the best timed variant and
+    the default variant is the library's automatic choice."""
     from fastload_gb300 import tuner
 
-    t = np.array([[2.0, 1.0, 4.0, 1.5, 3.0, 2.0], [1.0, 1.1, 1.2, 1.3, 1.4, 1.0]])
-    tg = tuner.targets(t)
-    np.testing.assert_allclose(tg[0], np.log2(t[0] / 1.0))
+    V = len(tuner.VARIANTS)
+    t = np.full((2, V), np.nan)
+    t[0, :4] = [2.0, 1.0, 4.0, 1.5]
+    t[1, :4] = [1.0, 1.1, 1.2, 1.3]
+    tg, m = tuner.targets(t), tuner.mask_of(t)
+    np.testing.assert_allclose(tg[0, :4], np.log2(t[0, :4] / 1.0))
+    assert np.all(tg[:, 4:] == 0) and np.all(m[:, 4:] == 0) and np.all(m[:, :4] == 1)
     ev = tuner.evaluate(np.array([1, 0]), t)
     assert ev["mean_regret"] == 0.0 and ev["frac_within_10pct"] == 1.0
+    assert tuner.DEFAULT == 0 and tuner.PLAIN == 1
     assert ev["speedup_vs_auto_rule"] == (2.0 + 1.0) / (1.0 + 1.0)
+
+
+def test_tuner_variant_table():
+    """The search space comes from the library (fl_tuner_variants): every
+    knob the tuner chooses -- heavy band, light item size, heavy loop, x
+    staging, units per warp, BF16 hi+lo storage -- takes more than one value,
+    and BF16 variants are offered to FP32 callers only."""
+    from fastload_gb300 import tuner
+
+    T = tuner.TABLE
+    assert len(T) == len(set(tuner.VARIANTS)) >= 60
+    for k in ("heavy_band", "light_item", "heavy_loop", "x_stage", "unit_warps", "value_type"):
+        assert len({o[k] for o in T}) >= 2, k
+    a64, a32 = tuner.allowed(0), tuner.allowed(1)
+    assert a64.sum() * 2 == a32.sum() == len(T)
+    assert all(o["value_type"] == tuner.TUNE_REQUESTED for o, ok in zip(T, a64) if ok)
 
 
 def test_tuner_specs_cover_the_families_and_ranges():
