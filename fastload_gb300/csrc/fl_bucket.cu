@@ -169,12 +169,11 @@ bool make_units(const std::vector<int> &sp, long per_unit, std::vector<int> &uni
 
 int bucket_auto_band(const int *sortnnz, int n, int nnz, cudaStream_t s, int x_bytes) {
     if (n <= 0 || nnz <= 0) return 0;
-    // FP64: 16,384 columns, 128 KB of x in shared memory beside the per-warp
-    // rings.  4-byte values: 49,152 columns, 192 KB of x (the packed band's
-    // register loop needs no ring, and a wider band leaves fewer nonzeros
-    // to the light part's latency-bound stream: at the 2^20-column Zipf(1.8)
-    // matrix 45.3 against 50.7 us back to back for 32,768 columns)
-    const int budget = x_bytes >= 8 ? BK_AUTO_BAND_BYTES : FM_SMEM_MAX;
+    // 16,384 columns of FP64 x, 32,768 of FP32 x: what fits 128 KB of shared
+    // memory beside the per-warp rings.  (A 192 KB band of FP32 x, without
+    // the rings, ran 64.1 against 50.8 us at the 2^20-column Zipf(1.8)
+    // matrix with the matrix's streams cold in L2.)
+    const int budget = BK_AUTO_BAND_BYTES;
     const int tail = std::min(n, budget / std::max(x_bytes, 1));
     std::vector<int> h(tail);
     FL_TRY(read_ints(s, sortnnz + (n - tail), h.data(), tail));
@@ -270,7 +269,12 @@ int build_bucket(Bucket &B, int m, int n, int nnz, const int *sortnnz, const int
     {
         std::vector<int> sp(H.nslices + 1), ustep, uslice;
         FL_TRY(read_ints(s, H.slice_ptr.get(), sp.data(), H.nslices + 1));
-        const long per_unit = (long)sp[H.nslices] / ((unit_warps > 0 ? unit_warps : 4L) * num_sms() * 32);
+        // a band of every column (no light part) takes two units a warp:
+        // fewer unit starts, each a chain of dependent loads (7-point
+        // Laplacian 128^3, FP32: 34.4 against 36.9 us; FP64 44.7 against
+        // 46.4 us; the Zipf(1.8) matrix as row slices 47.7 against 50.3 us)
+        const long uw = unit_warps > 0 ? unit_warps : (nh == n ? 2L : 4L);
+        const long per_unit = (long)sp[H.nslices] / (uw * num_sms() * 32);
         H.split = make_units(sp, per_unit, ustep, uslice);
         H.nunits = (int)uslice.size();
         FL_TRY(H.unit_step.alloc(ustep.size(), s));

@@ -155,7 +155,7 @@ int build_form(Form &F, const Layout &L, const fl_form_opts &o, cudaStream_t s) 
     F.wide = F.B.heavy.nh > 65535;
     // light items: as asked, else for 4-byte values at most 1,024 nonzeros
     // (the light stream's items are serial chains on one warp; beside the
-    // faster packed band, shorter chains end with it: 45.3 against 47.8 us
+    // faster packed band, shorter chains end with it: 50.8 against 54.3 us
     // at the 2^20-column Zipf(1.8) matrix)
     const int auto_item = item_nnz_for(nnz);
     const int item = o.light_item > 0 ? o.light_item : (vtype == FL_VALUES_F64 ? auto_item : std::min(auto_item, 1024));

@@ -135,22 +135,10 @@ __device__ __forceinline__ void emit_row32(int r, A p, Y *__restrict__ y, int la
     if ((lane == 31 || next != r) && r >= 0) atomicAdd(y + r, (Y)S);
 }
 
-// Bulk prefetch of [p, p + bytes) into L2 (p 16-byte aligned, bytes a
-// multiple of 16): one instruction, no registers, nothing waits for it.
-__device__ __forceinline__ void prefetch_l2(const void *p, uint32_t bytes) {
-    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
-}
-
-// Iterations of a work item whose rows and values are prefetched into L2
-// ahead of the one being loaded (0: none).
-constexpr int STREAM_PF = 0;
-
 // One work item; 4U rows of 32 nonzeros per warp iteration, all loads of an
 // iteration issued before any is used.  An item is a serial chain of up to
 // 16 iterations on one warp (a load of rows and values, then x gathers, then
-// the y updates); lane 0 keeps the rows and values of the next STREAM_PF
-// iterations on their way into L2 with bulk prefetches, so an iteration's
-// loads find them there instead of waiting for DRAM.
+// the y updates).
 template <typename V, typename Y, int U>
 __device__ __forceinline__ void stream_item(const ItemDesc &d, const RegionDesc *__restrict__ regions,
                                             const int *__restrict__ row, const V *__restrict__ val,
@@ -158,23 +146,10 @@ __device__ __forceinline__ void stream_item(const ItemDesc &d, const RegionDesc 
                                             int lane) {
     using A = typename VT<V>::A;
     constexpr int R = 4 * U;
-    // [e, min(e + 32R, end)) of both streams into L2: e is a multiple of 32,
-    // so both starts are 16-byte aligned; sizes round up to 16 bytes inside
-    // the streams' padding (at least FL_PAD entries past the last nonzero)
-    auto prefetch_iter = [&](int e) {
-        if (e < d.end) {
-            const uint32_t cnt = (uint32_t)min(32 * R, d.end - e);
-            prefetch_l2(row + e, (cnt * 4u + 15u) & ~15u);
-            prefetch_l2(val + e, (cnt * (uint32_t)sizeof(V) + 15u) & ~15u);
-        }
-    };
-    if (STREAM_PF > 0 && lane == 0)
-        for (int q = 1; q <= STREAM_PF; q++) prefetch_iter((d.begin & ~31) + 32 * R * q);
     const RegionDesc rg = regions[d.region];
     const int div = rg.div;
     const int s32 = rg.full ? 0 : 32 % div;  // partial chunk: column step per 32 nonzeros
     for (int e = d.begin & ~31; e < d.end; e += 32 * R) {
-        if (STREAM_PF > 0 && lane == 0) prefetch_iter(e + 32 * R * (STREAM_PF + 1));
         const int el0 = e + lane;
         int rw[R];
         A v[R];

@@ -52,7 +52,7 @@ std::vector<fl_form_opts> make_table() {
     for (int vt : {FL_TUNE_REQUESTED, FL_VALUES_BF16X2}) {
         add(vt, FL_BAND_AUTO, 0, FL_HEAVY_AUTO, FL_XSTAGE_AUTO, 0);
         for (int l : lights) add(vt, FL_BAND_NONE, l, FL_HEAVY_AUTO, FL_XSTAGE_AUTO, 0);
-        for (int u : {0, 2}) add(vt, FL_BAND_ALL, 0, FL_HEAVY_AUTO, FL_XSTAGE_AUTO, u);
+        for (int u : {0, 4}) add(vt, FL_BAND_ALL, 0, FL_HEAVY_AUTO, FL_XSTAGE_AUTO, u);
         for (int band : {8192, 24576, 49152})
             for (int l : lights) {
                 add(vt, band, l, FL_HEAVY_RING, FL_XSTAGE_AUTO, 0);

@@ -392,7 +392,8 @@ typedef struct fl_form_opts {
     int heavy_loop; /* FL_HEAVY_* */
     int x_stage;    /* FL_XSTAGE_* */
     int unit_warps; /* heavy-band work units per resident warp: 0 automatic
-                       (4), else 1..64 */
+                       (2 when the band holds every column, else 4),
+                       else 1..64 */
     int reserved;   /* must be 0 */
 } fl_form_opts;
 
