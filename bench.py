@@ -349,6 +349,20 @@ def measure_forms(fl, peak, reps=20):
                     sx = 8 if vt == fl.VALUES_F64 else 4
                     out[f"{cname}_{fname}_{bname}_k{k}"] = entry(
                         c, t, tc, k, sv, sx, yk.cpu().numpy(), ref[k], plain["gflops"])
+        # the learned tuner's pick for this matrix (through the C ABI), for
+        # FP64 and FP32 callers (an FP32 caller may get BF16 hi+lo storage)
+        for fname, vt, sv in forms[:2]:
+            picks = [q.add_tuned_form(vt) for q in plans]
+            fids = [f for f, _ in picks]
+            info = p.form_info(fids[0])
+            xk = p.permute_x_k(torch.from_numpy(xin[1]).cuda(), k=1, to_f32=info["value_type"] != fl.VALUES_F64)
+            yk = torch.empty(c.m, dtype=torch.float64, device="cuda")
+            calls = [lambda q=q, f=f: q.spmv_form(f, xk, yk) for q, f in zip(plans, fids)]
+            t = _time_b2b_ms(calls)
+            tc = _time_ms(calls[0], reps, flush)
+            d = entry(c, t, tc, 1, sv, 8 if vt == fl.VALUES_F64 else 4, yk.cpu().numpy(), ref[1], plain["gflops"])
+            d["tuned_variant"] = picks[0][1]
+            out[f"{cname}_{fname}_tuned_k1"] = d
         for q in plans:
             q.check()
             q.close()

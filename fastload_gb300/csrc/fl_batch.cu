@@ -112,6 +112,7 @@ int launch(fl_batch *b, const void *xs, void *y, cudaStream_t s) {
         a.x_ready = nullptr;
         a.x_epoch = 0;
         a.err_host = nullptr;
+        a.contig = 1;  // a block's units from one matrix at a time: its x in the SM's L1
     };
     if (b->vtype == FL_VALUES_F64) {
         FormArgs<double, double> a;

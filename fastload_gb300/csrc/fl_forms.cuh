@@ -70,6 +70,9 @@ struct FormArgs {
     // launch options of the form (host side: they pick the instantiation)
     int heavy_loop = FL_HEAVY_AUTO;
     int x_stage = FL_XSTAGE_AUTO;
+    // heavy units dealt to blocks in contiguous ranges (batches) rather
+    // than round-robin
+    int contig = 0;
 };
 
 // An expired bounded wait: bits into the launch's status word (and the host
@@ -769,17 +772,25 @@ __global__ void __launch_bounds__(FM_THREADS, 1) k_spmv_form(const FormArgs<V, Y
         // goes to block u % gridDim.x, so every block gets an even share of
         // both kinds; inside the block warps claim the block's units through
         // a shared-memory counter.  No global atomics, no per-launch reset.
+        // A batch (a.contig) deals its heavy units in one contiguous range
+        // per block instead, so a block's warps work on the same matrix and
+        // its x gathers share the SM's L1 (256 matrices of 186M nonzeros:
+        // 0.73 -> 0.64 ms; for a single matrix the round-robin deal is
+        // faster).
+        const int ml = a.nitems > b ? (a.nitems - 1 - b) / G + 1 : 0;  // this block's light items
+        const int hu = use_band ? a.nunits : 0;
+        const int h0 = (int)((long)b * hu / G);
+        const int nk = a.contig ? ml + (int)((long)(b + 1) * hu / G) - h0 : mine;
         for (;;) {
             int k = 0;
             if (lane == 0) k = atomicAdd(&claimed, 1);
             k = __shfl_sync(FULLM, k, 0);
-            if (k >= mine) break;
-            const int u = b + G * k;
-            if (u < a.nitems) {
-                light(u);
+            if (k >= nk) break;
+            if (k < ml) {
+                light(b + G * k);
                 continue;
             }
-            if (!heavy(u - a.nitems)) break;
+            if (!heavy(a.contig ? h0 + k - ml : b + G * k - a.nitems)) break;
         }
     } else {
         // The light columns' x is still arriving.  The block's units are
