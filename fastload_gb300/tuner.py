@@ -19,7 +19,9 @@ The training set: seeded matrices of five families (uniform rows, Zipf
 column degrees, banded, block-diagonal, row-skewed) generated on the GPU
 (fl_gen_fill), n log-uniform in [1e4, 4e6], nnz log-uniform in [1e5, 6e7],
 FP64 or FP32 values.  Every variant the matrix's caller may use is built
-and timed (calls back to back: the steady state of repeated SpMVs).  The
+and timed: calls back to back (the steady state of repeated SpMVs) for
+matrices whose streams can stay in L2 between calls, with L2 flushed before
+each call for larger ones.  The
 network (24 -> 64 -> 64 -> one output per variant, ReLU) regresses
 log2(t_variant / t_best), the variants a matrix may not use masked out, and
 is trained on the GPU by the library's own forward/backward/Adam kernels
@@ -170,22 +172,40 @@ def features(plan, value_type: int) -> np.ndarray:
 
 
 # ------------------------------------------------------------- autotune --
-def _time_calls(fn, reps: int) -> float:
+def _time_calls(fn, reps: int, flush=None) -> float:
     """Mean device ms of fn() over reps calls back to back (after two
     untimed); a device sleep ahead of the start event lets the host enqueue
-    the calls first, so small matrices are not timed at the host's pace."""
+    the calls first, so small matrices are not timed at the host's pace.
+    With `flush` (a tensor larger than L2) every call is preceded by a
+    write of it, whose own time, measured alone the same way, is taken off:
+    each call then starts with its matrix out of L2."""
     import torch
 
     fn()
     fn()
-    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    torch.cuda._sleep(600_000)
-    a.record()
-    for _ in range(reps):
-        fn()
-    b.record()
-    b.synchronize()
-    return a.elapsed_time(b) / reps
+
+    def run(body):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda._sleep(600_000)
+        a.record()
+        for _ in range(reps):
+            body()
+        b.record()
+        b.synchronize()
+        return a.elapsed_time(b)
+
+    if flush is None:
+        return run(fn) / reps
+    both = run(lambda: (flush.zero_(), fn()))
+    alone = run(flush.zero_)
+    return max(both - alone, 1e-4) / reps
+
+
+# Streams above this many bytes do not stay in L2 (129 MB) from one SpMV to
+# the next in practice (their own size, or the rest of an application's
+# working set, evicts them): such matrices are timed with L2 flushed between
+# calls; smaller ones back to back, as they run when repeated.
+COLD_BYTES = 48 << 20
 
 
 def autotune(plan, x, value_type: int, reps: int = 8) -> np.ndarray:
@@ -199,6 +219,9 @@ def autotune(plan, x, value_type: int, reps: int = 8) -> np.ndarray:
     ok = allowed(value_type)
     xs = {}
     y = torch.empty(plan.m, dtype=torch.float64, device="cuda")
+    nnz = plan.info["nnz"]
+    flush = (torch.empty(64 << 20, dtype=torch.float32, device="cuda")
+             if nnz * (8 if value_type == 0 else 4) + 4 * nnz > COLD_BYTES else None)
     groups: dict = {}
     for i, o in enumerate(TABLE):
         if ok[i]:
@@ -212,7 +235,7 @@ def autotune(plan, x, value_type: int, reps: int = 8) -> np.ndarray:
             xs[f32] = plan.permute_x_k(x, k=1, to_f32=f32)
         for i, heavy, xst in members:
             plan.set_form_launch(fid, heavy, xst)
-            times[i] = _time_calls(lambda: plan.spmv_form(fid, xs[f32], y), reps)
+            times[i] = _time_calls(lambda: plan.spmv_form(fid, xs[f32], y), reps, flush)
     plan.check()
     return times
 
