@@ -173,32 +173,34 @@ def features(plan, value_type: int) -> np.ndarray:
 
 # ------------------------------------------------------------- autotune --
 def _time_calls(fn, reps: int, flush=None) -> float:
-    """Mean device ms of fn() over reps calls back to back (after two
-    untimed); a device sleep ahead of the start event lets the host enqueue
-    the calls first, so small matrices are not timed at the host's pace.
-    With `flush` (a tensor larger than L2) every call is preceded by a
-    write of it, whose own time, measured alone the same way, is taken off:
-    each call then starts with its matrix out of L2."""
+    """Device ms of one fn() call.  Without `flush`: the mean over reps
+    calls back to back (after two untimed), a device sleep ahead of the
+    start event letting the host enqueue the calls first, so small matrices
+    are not timed at the host's pace.  With `flush` (a tensor larger than
+    L2): the median over reps single calls, each after a write of the flush
+    tensor, so each starts with its matrix out of L2."""
     import torch
 
     fn()
     fn()
-
-    def run(body):
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    if flush is None:
         torch.cuda._sleep(600_000)
         a.record()
         for _ in range(reps):
-            body()
+            fn()
         b.record()
         b.synchronize()
-        return a.elapsed_time(b)
-
-    if flush is None:
-        return run(fn) / reps
-    both = run(lambda: (flush.zero_(), fn()))
-    alone = run(flush.zero_)
-    return max(both - alone, 1e-4) / reps
+        return a.elapsed_time(b) / reps
+    ts = []
+    for _ in range(reps):
+        flush.zero_()
+        a.record()
+        fn()
+        b.record()
+        b.synchronize()
+        ts.append(a.elapsed_time(b))
+    return float(np.median(ts))
 
 
 # Streams above this many bytes do not stay in L2 (129 MB) from one SpMV to
@@ -250,6 +252,14 @@ def collect(count: int, seed: int = 5, out: str | None = None, log_every: int = 
                 "T": np.array(T, np.float64).reshape(-1, len(TABLE)),
                 "meta": np.array([json.dumps(m) for m in meta]), "variants": np.array(VARIANTS)}
 
+    # one untimed round on a small matrix first: the first launches of each
+    # kernel pay one-time costs (module loading, shared-memory opt-in)
+    warm, _, xw = make_plan({"family": "uniform", "n": 20000, "m": 20000, "nnz_target": 2e5, "seed": 1,
+                             "values": 1, "param": 0.0})
+    try:
+        autotune(warm, xw, 1, reps=2)
+    finally:
+        warm.close()
     for i in range(count):
         spec = sample_spec(rng, i)
         plan, nnz, x = make_plan(spec)
