@@ -19,9 +19,10 @@ The training set: seeded matrices of five families (uniform rows, Zipf
 column degrees, banded, block-diagonal, row-skewed) generated on the GPU
 (fl_gen_fill), n log-uniform in [1e4, 4e6], nnz log-uniform in [1e5, 6e7],
 FP64 or FP32 values.  Every variant the matrix's caller may use is built
-and timed: calls back to back (the steady state of repeated SpMVs) for
-matrices whose streams can stay in L2 between calls, with L2 flushed before
-each call for larger ones.  The
+and timed with calls back to back (the steady state of repeated SpMVs):
+on one plan for matrices whose streams can stay in L2 between calls,
+alternating between two copies of the plan for larger ones, so that their
+calls find the matrix out of L2.  The
 network (24 -> 64 -> 64 -> one output per variant, ReLU) regresses
 log2(t_variant / t_best), the variants a matrix may not use masked out, and
 is trained on the GPU by the library's own forward/backward/Adam kernels
@@ -139,9 +140,10 @@ def degrees(spec: dict) -> np.ndarray:
     return d
 
 
-def make_plan(spec: dict, heavy_band: int = -1):
+def make_plan(spec: dict, heavy_band: int = -1, copies: int = 1):
     """Generates the spec's matrix on the GPU and builds its plan.
-    Returns (plan, nnz, device x)."""
+    Returns (plan, nnz, device x); with copies > 1 the plan is a list of
+    that many plans of the same matrix."""
     import torch
 
     from .plan import Plan
@@ -157,12 +159,19 @@ def make_plan(spec: dict, heavy_band: int = -1):
                              C.c_void_p(rows.data_ptr()), C.c_void_p(vals.data_ptr()), float(spec["param"]),
                              C.c_ulonglong(spec["seed"] & ((1 << 64) - 1)), None))
     torch.cuda.synchronize()
-    plan = Plan.from_csc(spec["m"], spec["n"], cp, rows[:nnz], vals[:nnz], heavy_band=heavy_band)
+    plans = [Plan.from_csc(spec["m"], spec["n"], cp, rows[:nnz], vals[:nnz], heavy_band=heavy_band)
+             for _ in range(copies)]
     g = torch.Generator(device="cuda")
     g.manual_seed(spec["seed"] & 0x7FFFFFFF)
     x = torch.rand(spec["n"], dtype=torch.float64, device="cuda", generator=g) * 2 - 1
     del rows, vals, cp
-    return plan, nnz, x
+    return (plans[0] if copies == 1 else plans), nnz, x
+
+
+def is_large(nnz: int, value_type: int) -> bool:
+    """Streams too large to stay in L2 between one SpMV and the next in
+    practice (COLD_BYTES)."""
+    return nnz * ((8 if value_type == 0 else 4) + 4) > COLD_BYTES
 
 
 def features(plan, value_type: int) -> np.ndarray:
@@ -172,58 +181,49 @@ def features(plan, value_type: int) -> np.ndarray:
 
 
 # ------------------------------------------------------------- autotune --
-def _time_calls(fn, reps: int, flush=None) -> float:
-    """Device ms of one fn() call.  Without `flush`: the mean over reps
-    calls back to back (after two untimed), a device sleep ahead of the
-    start event letting the host enqueue the calls first, so small matrices
-    are not timed at the host's pace.  With `flush` (a tensor larger than
-    L2): the median over reps single calls, each after a write of the flush
-    tensor, so each starts with its matrix out of L2."""
+def _time_calls(fns, reps: int) -> float:
+    """Mean device ms of one call over reps calls back to back, cycling
+    through fns (one callable per copy of the matrix: with two copies each
+    call finds its matrix evicted from L2 by the other's call), after two
+    untimed rounds; a device sleep ahead of the start event lets the host
+    enqueue the calls first, so small matrices are not timed at the host's
+    pace."""
     import torch
 
-    fn()
-    fn()
+    for f in fns * 2:
+        f()
     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    if flush is None:
-        torch.cuda._sleep(600_000)
-        a.record()
-        for _ in range(reps):
-            fn()
-        b.record()
-        b.synchronize()
-        return a.elapsed_time(b) / reps
-    ts = []
-    for _ in range(reps):
-        flush.zero_()
-        a.record()
-        fn()
-        b.record()
-        b.synchronize()
-        ts.append(a.elapsed_time(b))
-    return float(np.median(ts))
+    torch.cuda._sleep(600_000)
+    a.record()
+    for i in range(reps):
+        fns[i % len(fns)]()
+    b.record()
+    b.synchronize()
+    return a.elapsed_time(b) / reps
 
 
 # Streams above this many bytes do not stay in L2 (129 MB) from one SpMV to
 # the next in practice (their own size, or the rest of an application's
-# working set, evicts them): such matrices are timed with L2 flushed between
-# calls; smaller ones back to back, as they run when repeated.
+# working set, evicts them): such matrices are timed alternating between two
+# copies of their plan; smaller ones back to back on one, as they run when
+# repeated.
 COLD_BYTES = 48 << 20
 
 
-def autotune(plan, x, value_type: int, reps: int = 8) -> np.ndarray:
+def autotune(plans, x, value_type: int, reps: int = 8) -> np.ndarray:
     """Exhaustive over the variant table: every variant value_type's caller
     may use is built as a form of the plan (variants that differ only in
-    launch options share one build) and timed.  Returns ms per variant, NaN
-    where the variant is not allowed."""
+    launch options share one build) and timed.  plans: a plan, or a list of
+    plans of the same matrix whose calls alternate (large matrices).
+    Returns ms per variant, NaN where the variant is not allowed."""
     import torch
 
+    plans = plans if isinstance(plans, list) else [plans]
+    p0 = plans[0]
     times = np.full(len(TABLE), np.nan)
     ok = allowed(value_type)
     xs = {}
-    y = torch.empty(plan.m, dtype=torch.float64, device="cuda")
-    nnz = plan.info["nnz"]
-    flush = (torch.empty(64 << 20, dtype=torch.float32, device="cuda")
-             if nnz * (8 if value_type == 0 else 4) + 4 * nnz > COLD_BYTES else None)
+    y = torch.empty(p0.m, dtype=torch.float64, device="cuda")
     groups: dict = {}
     for i, o in enumerate(TABLE):
         if ok[i]:
@@ -231,14 +231,17 @@ def autotune(plan, x, value_type: int, reps: int = 8) -> np.ndarray:
             key = (r["value_type"], r["heavy_band"], r["light_item"], r["unit_warps"])
             groups.setdefault(key, []).append((i, r["heavy_loop"], r["x_stage"]))
     for (vt, band, light, units), members in groups.items():
-        fid = plan.add_form(vt, band, light_item=light, unit_warps=units)
+        fids = [p.add_form(vt, band, light_item=light, unit_warps=units) for p in plans]
         f32 = vt != 0
         if f32 not in xs:
-            xs[f32] = plan.permute_x_k(x, k=1, to_f32=f32)
+            xs[f32] = p0.permute_x_k(x, k=1, to_f32=f32)
+        fns = [lambda p=p, f=f: p.spmv_form(f, xs[f32], y) for p, f in zip(plans, fids)]
         for i, heavy, xst in members:
-            plan.set_form_launch(fid, heavy, xst)
-            times[i] = _time_calls(lambda: plan.spmv_form(fid, xs[f32], y), reps, flush)
-    plan.check()
+            for p, f in zip(plans, fids):
+                p.set_form_launch(f, heavy, xst)
+            times[i] = _time_calls(fns, reps)
+    for p in plans:
+        p.check()
     return times
 
 
@@ -255,19 +258,23 @@ def collect(count: int, seed: int = 5, out: str | None = None, log_every: int = 
     # one untimed round on a small matrix first: the first launches of each
     # kernel pay one-time costs (module loading, shared-memory opt-in)
     warm, _, xw = make_plan({"family": "uniform", "n": 20000, "m": 20000, "nnz_target": 2e5, "seed": 1,
-                             "values": 1, "param": 0.0})
+                             "values": 1, "param": 0.0}, copies=2)
     try:
         autotune(warm, xw, 1, reps=2)
     finally:
-        warm.close()
+        for p in warm:
+            p.close()
     for i in range(count):
         spec = sample_spec(rng, i)
-        plan, nnz, x = make_plan(spec)
+        copies = 2 if is_large(int(degrees(spec).sum()), spec["values"]) else 1
+        plans, nnz, x = make_plan(spec, copies=copies)
+        plans = plans if isinstance(plans, list) else [plans]
         try:
-            f = features(plan, spec["values"])
-            t = autotune(plan, x, spec["values"])
+            f = features(plans[0], spec["values"])
+            t = autotune(plans, x, spec["values"])
         finally:
-            plan.close()
+            for p in plans:
+                p.close()
         X.append(f)
         T.append(t)
         meta.append(dict(spec, nnz=nnz))
