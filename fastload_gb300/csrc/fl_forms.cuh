@@ -414,6 +414,7 @@ constexpr int P4_VB = 32 * 4 * 4;           // value bytes of a pack (512)
 constexpr int P4_CB = 32 * 4 * 2;           // 16-bit column bytes of a pack (256)
 constexpr int P4_SB = P4_VB + P4_CB;        // ring stage
 constexpr int P4_RING_WARP = P4_STAGES * P4_SB;
+static_assert((P4_STAGES & (P4_STAGES - 1)) == 0, "ring slots are taken modulo a power of two");
 
 __host__ __device__ __forceinline__ long p4_index(long S, int l) { return 128 * (S >> 2) + 4 * l + (S & 3); }
 // Entries of a packed band array of `steps` steps: whole packs, plus one
