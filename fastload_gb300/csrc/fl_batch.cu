@@ -258,9 +258,12 @@ int fl_batch_create(fl_batch_t *out, int count, const fl_plan_t *plans, int valu
         b->val = std::move(pv);
         b->col = std::move(pc);
     }
-    // work units over the stacked slices, about four per resident warp
+    // work units over the stacked slices, about sixteen per resident warp:
+    // a block's contiguous range of units is claimed unit by unit, so
+    // smaller units even out its warps' work (256 matrices of 186M
+    // nonzeros: 0.82 / 0.67 / 0.64 / 0.62 / 0.60 ms at 1 / 2 / 4 / 8 / 16)
     std::vector<int> ustep, uslice;
-    b->split = make_units(sp, e_off[count] / (4L * num_sms() * 32), ustep, uslice);
+    b->split = make_units(sp, e_off[count] / (16L * num_sms() * 32), ustep, uslice);
     b->nunits = (int)uslice.size();
     FL_TRY(b->unit_step.alloc(ustep.size(), s));
     FL_TRY(b->unit_slice.alloc(std::max<size_t>(uslice.size(), 1), s));
