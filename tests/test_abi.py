@@ -100,6 +100,15 @@ def test_argument_errors_without_gpu(built_lib):
     h = C.c_void_p()
     rc = built_lib.fl_plan_create_csr(C.byref(h), 2, 2, 1, None, None, None, 0, None)
     assert rc == -1 and not h.value
+    # the calls added beside the reference's: argument checks before any GPU work
+    assert built_lib.fl_convert_values(0, 4, None, None, None) == -1  # FP64 is not a storage conversion
+    assert built_lib.fl_convert_values(1, -1, None, None, None) == -1
+    assert built_lib.fl_convert_values(2, 0, None, None, None) == 0  # nothing to convert
+    fid = C.c_int(-1)
+    assert built_lib.fl_plan_add_form_opts(None, None, C.byref(fid)) == -1
+    assert built_lib.fl_plan_form_set_launch(None, 0, 1, 0) == -1
+    assert built_lib.fl_plan_add_tuned_form(None, b"model", 1, 0, C.byref(fid), None) == -1
+    assert built_lib.fl_tuner_variants(None, 0) > 0
 
 
 def test_python_wrappers_raise(built_lib):

@@ -74,3 +74,29 @@ def test_tuner_specs_cover_the_families_and_ranges():
         assert d.shape == (s["n"],) and d.min() >= 0 and d.sum() <= tuner.NNZ_RANGE[1] * 1.06
         if s["family"] == "banded":
             assert d.max() <= max(1, int(s["param"]))
+
+
+def test_committed_model_and_data_match_the_variant_table():
+    """The committed tuner model (the library's format, which
+    fl_plan_add_tuned_form reads) and autotuner data were made over the
+    library's current variant table: magic, shape, the table itself, and a
+    file size that matches the shape.  Read without a GPU."""
+    import os
+
+    from fastload_gb300 import tuner
+
+    raw = open(tuner.MODEL, "rb").read()
+    assert raw[:8] == b"FLTUNER1"
+    n_in, h1, h2, n_out, nv = (int(v) for v in np.frombuffer(raw, "<i4", 5, 8))
+    assert (n_in, n_out, nv) == (24, len(tuner.TABLE), len(tuner.TABLE))
+    n_params = n_in * h1 + h1 + h1 * h2 + h2 + h2 * n_out + n_out
+    assert len(raw) == 40 + 4 * (2 * n_in + n_params) + 32 * nv
+    opts = np.frombuffer(raw, "<i4", 8 * nv, len(raw) - 32 * nv).reshape(nv, 8)
+    fields = ("value_type", "heavy_band", "y_f32", "light_item", "heavy_loop", "x_stage", "unit_warps", "reserved")
+    assert [dict(zip(fields, map(int, r))) for r in opts] == tuner.TABLE
+    data = os.path.join(os.path.dirname(tuner.MODEL), "cfg5_autotune.npz")
+    with np.load(data) as z:
+        assert tuple(str(v) for v in z["variants"]) == tuner.VARIANTS
+        T = z["T"]
+        assert T.shape == (2200, len(tuner.TABLE))
+        assert np.all(np.isfinite(T) | np.isnan(T)) and np.nanmin(T) > 0
