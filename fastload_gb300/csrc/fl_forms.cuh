@@ -9,9 +9,10 @@
 //      or from global memory (bands wider than shared memory);
 //   C16 heavy-band column indices stored as 16 bits (band <= 65535) or 32;
 //   Y  y type (double, or float for the FP32-accumulating batched form);
-//   RING the band's values and columns streamed through per-warp
-//      shared-memory rings (K = 1, x in shared memory) instead of the
-//      register-pipelined loop;
+//   RING the band's values and columns streamed through shared-memory rings
+//      filled by cp.async (K = 1, x in shared memory) instead of the
+//      register-pipelined loop: per warp for FP64 bands, per lane for the
+//      4-byte bands kept in packs of four steps;
 //   OVL the light columns' x still arriving when the kernel starts (the
 //      overlapped host-buffer call): heavy units first, light items once a
 //      flag says the x is in.
@@ -24,7 +25,8 @@
 // atomic per run (K = 1) or per (nonzero, rhs) (K > 1), the heavy band in
 // 32-row slices with one lane per row.  When the band holds every column
 // (no light part) each row is owned by one lane and y is updated without
-// atomics.
+// atomics.  Heavy units are dealt to blocks round-robin, or in contiguous
+// ranges for batches (FormArgs::contig).
 #pragma once
 
 #include "fl_stream.cuh"
