@@ -555,7 +555,7 @@ int fl_plan_info_get(fl_plan_t p, fl_plan_info *info) {
         const Layout &Q = B.light;
         b += Q.row.n * 4 + Q.val.n * 8 + Q.regions.region.n * sizeof(RegionDesc) +
              Q.regions.item.n * sizeof(ItemDesc) + 5 * (size_t)(Q.st.steps + 1) * 4;
-        b += H.val.n * 8 + H.col.n * 2 + H.slice_ptr.n * 4 + H.row.n * 4 + H.len.n * 4;
+        b += H.val.n * 8 + H.col.n * 2 + H.col32.n * 4 + H.slice_ptr.n * 4 + H.row.n * 4 + H.len.n * 4;
     }
     info->device_bytes = b;
     return FL_SUCCESS;

@@ -411,7 +411,7 @@ __device__ __forceinline__ void heavy_unit_ring(const FormArgs<V, Y> &a, int sl,
 // does not have (a lane past its row's length inside a slice) hold value 0
 // and column nh, and the shared-memory staging of x keeps a zero at x[nh],
 // so the ring loop needs no length test.
-constexpr int P4_STAGES = 2;                // packs in a lane's ring (a power of two)
+constexpr int P4_STAGES = 4;                // packs in a lane's ring (a power of two)
 constexpr int P4_VB = 32 * 4 * 4;           // value bytes of a pack (512)
 constexpr int P4_CB = 32 * 4 * 2;           // 16-bit column bytes of a pack (256)
 constexpr int P4_SB = P4_VB + P4_CB;        // ring stage
