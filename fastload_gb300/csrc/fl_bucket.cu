@@ -350,7 +350,8 @@ int spmv_bucket_f64(const Bucket &B, const double *xs, double *y, int accumulate
     // zeroing first when every row has band nonzeros
     const int m = B.light.m;
     a.heavy_mode = (R.nitems > 0 || H.split) ? 0 : (!accumulate && H.nrows == m ? 2 : 1);
-    if (!accumulate && a.heavy_mode != 2) FL_TRY(zero_device(y, (size_t)m * sizeof(double), s));
+    a.after_zeroing = !accumulate && a.heavy_mode != 2;
+    if (a.after_zeroing) FL_TRY(zero_device(y, (size_t)m * sizeof(double), s));
     const size_t bytes = (size_t)a.nh * sizeof(double);
     a.bulk = a.nh > 0 && ((uintptr_t)(xs + H.H0) % 16 == 0) && bytes % 16 == 0;
     if (a.nitems == 0 && a.nunits == 0) return FL_SUCCESS;

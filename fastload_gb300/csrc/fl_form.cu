@@ -225,7 +225,8 @@ int spmv_form(Form &F, int k, const void *xs, void *y, int accumulate, cudaStrea
     // written without zeroing first when every row has band nonzeros
     const bool light = B.light.regions.nitems > 0;
     const int mode = (light || B.heavy.split) ? 0 : (!accumulate && B.heavy.nrows == m ? 2 : 1);
-    if (!accumulate && mode != 2) FL_TRY(zero_device(y, (size_t)m * k * ysz, s));
+    const bool zeroed = !accumulate && mode != 2;
+    if (zeroed) FL_TRY(zero_device(y, (size_t)m * k * ysz, s));
     if (!light && B.heavy.nnz == 0) return FL_SUCCESS;
     const HeavyBand &H = B.heavy;
     const size_t band_bytes = (size_t)H.nh * k * xsz;
@@ -235,6 +236,7 @@ int spmv_form(Form &F, int k, const void *xs, void *y, int accumulate, cudaStrea
         auto a = form_args<double, double>(F, B.light.val.get(), B.heavy.val.get(), xs, y);
         a.bulk = bulk;
         a.heavy_mode = mode;
+        a.after_zeroing = zeroed;
         return run_form_f64(a, k, F.wide, s);
     }
     if (F.vtype == FL_VALUES_F32) {
@@ -242,16 +244,19 @@ int spmv_form(Form &F, int k, const void *xs, void *y, int accumulate, cudaStrea
             auto a = form_args<float, float>(F, (const float *)F.lval.get(), (const float *)F.hval.get(), xs, y);
             a.bulk = bulk;
             a.heavy_mode = mode;
+            a.after_zeroing = zeroed;
             return run_form_f32_y32(a, k, F.wide, s);
         }
         auto a = form_args<float, double>(F, (const float *)F.lval.get(), (const float *)F.hval.get(), xs, y);
         a.bulk = bulk;
         a.heavy_mode = mode;
+        a.after_zeroing = zeroed;
         return run_form_f32(a, k, F.wide, s);
     }
     auto a = form_args<bf16x2_t, double>(F, (const bf16x2_t *)F.lval.get(), (const bf16x2_t *)F.hval.get(), xs, y);
     a.bulk = bulk;
     a.heavy_mode = mode;
+    a.after_zeroing = zeroed;
     return run_form_bf16(a, k, F.wide, s);
 }
 

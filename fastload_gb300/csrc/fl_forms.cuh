@@ -75,6 +75,10 @@ struct FormArgs {
     // heavy units dealt to blocks in contiguous ranges (batches) rather
     // than round-robin
     int contig = 0;
+    // the kernel launched just before this one is the library's y zeroing
+    // (which releases its dependent only after its own wait for everything
+    // before it): the band's x may be staged before waiting for it
+    int after_zeroing = 0;
 };
 
 // An expired bounded wait: bits into the launch's status word (and the host
@@ -686,10 +690,14 @@ __global__ void __launch_bounds__(FM_THREADS, 1) k_spmv_form(const FormArgs<V, Y
     const int tid = threadIdx.x, lane = tid & 31;
     const uint32_t bar = (uint32_t)__cvta_generic_to_shared(&mbar);
     if (tid == 0) claimed = claimed_h = x_in = 0;
-    // Launched as a programmatic dependent of the kernel before it (the y
-    // zeroing): the block may be resident before that kernel ends, so wait
-    // for it before reading or writing anything.
-    asm volatile("griddepcontrol.wait;" ::: "memory");
+    // Launched as a programmatic dependent of the kernel before it: the
+    // block may be resident before that kernel ends, so it waits for it
+    // before reading or writing anything -- except, when that kernel is the
+    // library's y zeroing, the staging of the band's x, which then runs
+    // beside the zeroing: the zeroing kernel releases this one only after
+    // its own wait for every kernel before it, so x is complete, and the
+    // staging writes shared memory only.
+    if (!a.after_zeroing) asm volatile("griddepcontrol.wait;" ::: "memory");
     const bool use_band = a.nh > 0 && a.nslices > 0;
     if (XS && use_band) {
         const uint32_t bytes = (uint32_t)a.nh * K * (uint32_t)sizeof(X);
@@ -721,6 +729,7 @@ __global__ void __launch_bounds__(FM_THREADS, 1) k_spmv_form(const FormArgs<V, Y
             __syncthreads();
         }
     }
+    if (a.after_zeroing) asm volatile("griddepcontrol.wait;" ::: "memory");
     const X *xsrc = XS ? (const X *)xh : a.xs + (size_t)a.H0 * K;
     const int total = a.nitems + (use_band ? a.nunits : 0);
     bool staged = !(XS && use_band && a.bulk);
