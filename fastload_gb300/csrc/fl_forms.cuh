@@ -693,11 +693,16 @@ __global__ void __launch_bounds__(FM_THREADS, 1) k_spmv_form(const FormArgs<V, Y
     // Launched as a programmatic dependent of the kernel before it: the
     // block may be resident before that kernel ends, so it waits for it
     // before reading or writing anything -- except, when that kernel is the
-    // library's y zeroing, the staging of the band's x, which then runs
-    // beside the zeroing: the zeroing kernel releases this one only after
-    // its own wait for every kernel before it, so x is complete, and the
-    // staging writes shared memory only.
-    if (!a.after_zeroing) asm volatile("griddepcontrol.wait;" ::: "memory");
+    // library's y zeroing, for what does not touch y: the staging of the
+    // band's x and the first loads of the light items then run beside the
+    // zeroing (the zeroing kernel releases this one only after its own wait
+    // for every kernel before it, so x is complete), and each thread waits
+    // before its first y update (pdl_wait_once; heavy units wait once the
+    // staged x is in) and, at the latest, before it exits.  Kernels without
+    // a staged band wait at once (their register budget is spent on the
+    // band loop).
+    bool waited = !(XS && a.after_zeroing);
+    if (waited) asm volatile("griddepcontrol.wait;" ::: "memory");
     const bool use_band = a.nh > 0 && a.nslices > 0;
     if (XS && use_band) {
         const uint32_t bytes = (uint32_t)a.nh * K * (uint32_t)sizeof(X);
@@ -729,7 +734,6 @@ __global__ void __launch_bounds__(FM_THREADS, 1) k_spmv_form(const FormArgs<V, Y
             __syncthreads();
         }
     }
-    if (a.after_zeroing) asm volatile("griddepcontrol.wait;" ::: "memory");
     const X *xsrc = XS ? (const X *)xh : a.xs + (size_t)a.H0 * K;
     const int total = a.nitems + (use_band ? a.nunits : 0);
     bool staged = !(XS && use_band && a.bulk);
@@ -760,6 +764,7 @@ __global__ void __launch_bounds__(FM_THREADS, 1) k_spmv_form(const FormArgs<V, Y
             }
             staged = true;
         }
+        if constexpr (XS) pdl_wait_once(&waited);
         const int sl = __ldg(a.unit_slice + ui), T0 = __ldg(a.unit_step + ui), T1 = __ldg(a.unit_step + ui + 1);
         // the rings start past x and its 16 bytes of zeros (x[nh])
         const size_t xb = ((size_t)a.nh * K * sizeof(X) + 16 + 127) & ~(size_t)127;
@@ -776,8 +781,12 @@ __global__ void __launch_bounds__(FM_THREADS, 1) k_spmv_form(const FormArgs<V, Y
         return true;
     };
     auto light = [&](int u) {
-        if constexpr (K == 1) stream_item<V, Y, 1>(a.items[u], a.regions, a.row, a.val, a.xs, a.y, lane);
-        else light_item_kn<V, K, Y>(a.items[u], a.regions, a.row, a.val, a.xs, a.y, lane);
+        if constexpr (K == 1) {
+            stream_item<V, Y, 1>(a.items[u], a.regions, a.row, a.val, a.xs, a.y, lane, XS ? &waited : nullptr);
+        } else {
+            if constexpr (XS) pdl_wait_once(&waited);
+            light_item_kn<V, K, Y>(a.items[u], a.regions, a.row, a.val, a.xs, a.y, lane);
+        }
     };
     if constexpr (!OVL) {
         // Work distribution: unit u (light items first, then heavy units)
@@ -893,6 +902,9 @@ __global__ void __launch_bounds__(FM_THREADS, 1) k_spmv_form(const FormArgs<V, Y
         }
         if (!ok && lane == 0) form_fail(a, 2);
     }
+    // every thread has waited for the kernel before this one (a warp that
+    // found no work has not yet), so this kernel never completes before it
+    if constexpr (XS) pdl_wait_once(&waited);
     // this block is done: a dependent launch behind this kernel may start
     // (it waits for this kernel's completion before touching memory)
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");

@@ -111,9 +111,20 @@ struct VT<bf16x2_t> {
     static __device__ __forceinline__ A from_bits(uint32_t u) { return bf16x2_decode(u); }
 };
 
+// Waits (once per thread) for the kernel this one is a programmatic
+// dependent of, before the thread's first y update; *waited is the thread's
+// flag, nullptr: nothing to wait for.
+__device__ __forceinline__ void pdl_wait_once(bool *waited) {
+    if (waited && !*waited) {
+        asm volatile("griddepcontrol.wait;" ::: "memory");
+        *waited = true;
+    }
+}
+
 // y[r] += p for one 32-nonzero row of the stream (r = -1: no nonzero).
 template <typename A, typename Y>
-__device__ __forceinline__ void emit_row32(int r, A p, Y *__restrict__ y, int lane) {
+__device__ __forceinline__ void emit_row32(int r, A p, Y *__restrict__ y, int lane, bool *waited = nullptr) {
+    pdl_wait_once(waited);
     const int prev = __shfl_up_sync(FULLM, r, 1);
     const bool join = lane > 0 && r >= 0 && prev == r;
     if (!__any_sync(FULLM, join)) {
@@ -139,11 +150,13 @@ __device__ __forceinline__ void emit_row32(int r, A p, Y *__restrict__ y, int la
 // iteration issued before any is used.  An item is a serial chain of up to
 // 16 iterations on one warp (a load of rows and values, then x gathers, then
 // the y updates).
+// waited: see pdl_wait_once (the first iteration's loads are issued before
+// the wait).
 template <typename V, typename Y, int U>
 __device__ __forceinline__ void stream_item(const ItemDesc &d, const RegionDesc *__restrict__ regions,
                                             const int *__restrict__ row, const V *__restrict__ val,
                                             const typename VT<V>::X *__restrict__ xs, Y *__restrict__ y,
-                                            int lane) {
+                                            int lane, bool *waited = nullptr) {
     using A = typename VT<V>::A;
     constexpr int R = 4 * U;
     const RegionDesc rg = regions[d.region];
@@ -196,7 +209,7 @@ __device__ __forceinline__ void stream_item(const ItemDesc &d, const RegionDesc 
             const int el = el0 + 32 * k;
             const bool valid = el >= d.begin && el < d.end;
             if (k > 0 && !fresh[k]) xv[k] = xv[k - 1];
-            emit_row32<A, Y>(valid ? rw[k] : -1, valid ? v[k] * (A)xv[k] : (A)0, y, lane);
+            emit_row32<A, Y>(valid ? rw[k] : -1, valid ? v[k] * (A)xv[k] : (A)0, y, lane, waited);
         }
     }
 }
