@@ -477,9 +477,11 @@ def measure_comparators(fl, c, x, ydd, B, reps=20):
 
 def run_profile(spec):
     """--profile case:values:band:k -- builds one case and runs one kernel a
-    few times (for ncu captures).  case lap128 | zipf | zipf<n>; values
-    f64 | f32 | bf16x2 | plain (the plain FP64 stream kernel) | bucket (the
-    FP64 bucketed kernel); band auto | none | all | <columns>; k 1 | 8."""
+    few times (for ncu captures).  case lap128 | zipf | zipf<n> | batch (the
+    256-matrix batch of the batch line, FP32 values and y; values and band
+    are ignored); values f64 | f32 | bf16x2 | plain (the plain FP64 stream
+    kernel) | bucket (the FP64 bucketed kernel); band auto | none | all |
+    <columns>; k 1 | 8."""
     import torch
 
     import fastload_gb300 as fl
@@ -487,6 +489,17 @@ def run_profile(spec):
 
     case, vals, band, k = spec.split(":")
     k = int(k)
+    if case == "batch":
+        mats = gen.batch(256, seed=3, dtype=np.float64)
+        plans = [fl.Plan.from_csc(c.m, c.n, c.colptr, c.rowidx, c.val) for c in mats]
+        with fl.Batch(plans, value_type=fl.VALUES_F32, y_f32=True) as b:
+            for p in plans:
+                p.close()
+            xs = b.permute_x(torch.from_numpy(np.concatenate([c.x for c in mats])).cuda())
+            y = torch.empty(b.m, dtype=torch.float32, device="cuda")
+            ms = _time_ms(lambda: b.spmv(xs, y), 5)
+        print(json.dumps({"profile": spec, "nnz": int(sum(c.nnz for c in mats)), "ms": ms}), flush=True)
+        return
     if case == "lap128":
         c = gen.laplacian7(128, seed=4)
     else:
