@@ -16,9 +16,12 @@
 //   OVL the light columns' x still arriving when the kernel starts (the
 //      overlapped host-buffer call): heavy units first, light items once a
 //      flag says the x is in.
-// Launched as a programmatic dependent of the kernel before it (the y
-// zeroing), the kernel waits for that kernel before touching memory and
-// releases its own dependent when each block is done.
+// Launched as a programmatic dependent of the kernel before it, the kernel
+// waits for that kernel before touching memory -- or, behind the library's
+// own y zeroing (FormArgs::after_zeroing, kernels with a staged band), before
+// each thread's first y update, so the band's x staging and the light
+// items' first loads overlap the zeroing -- and releases its own dependent
+// when each block is done.
 // Products and per-row sums are computed in FP32 for the FP32/BF16 forms and
 // in FP64 for the FP64 form; y is accumulated in Y.  The work is the bucketed
 // split of fl_bucket.cu: light columns in the FastLoad tile stream with one
