@@ -157,8 +157,11 @@ __device__ __forceinline__ void heavy_load_group(const FormArgs<V, Y> &a, int ba
         if (j0 + g < len) {
             const int idx = base + 32 * (j0 + g) + lane;
             v[g] = VT<V>::stream1(a.hval + idx);
-            if constexpr (C16) c[g] = (int)__ldg(a.hcol16 + idx);
-            else c[g] = __ldg(a.hcol32 + idx);
+            // columns streamed too (evict-first): allocated normally in L1
+            // they evicted the x lines the gathers reuse (7-point Laplacian
+            // 128^3, FP64 band of every column: 45.5 -> 41.4 us)
+            if constexpr (C16) c[g] = (int)__ldcs(a.hcol16 + idx);
+            else c[g] = __ldcs(a.hcol32 + idx);
         }
     }
 }
